@@ -1,0 +1,195 @@
+/*
+ * mgpu_gb300.h - C ABI of the GB300 (sm_103a) data-parallel primitives.
+ *
+ * These entry points replace the host calls of seanbaxter/mgpu-shaders'
+ * Vulkan API (inc/mgpu/vk/*.hxx).  Every primitive keeps the reference's
+ * two-phase auxiliary-memory protocol:
+ *
+ *   size_t aux_size = 0;
+ *   mgpu_radix_sort(ctx, ..., NULL, &aux_size);   // only adds the bytes needed
+ *   void* aux = <device allocation of aux_size bytes>;
+ *   mgpu_radix_sort(ctx, ..., aux, &aux_size);    // runs; aux_size = capacity
+ *
+ * as in vk/merge.hxx:30-34, vk/mergesort.hxx:35-41, vk/scan.hxx:19-22,54-59
+ * and vk/radix.hxx:288-302 (where `aux_data == nullptr` only grows aux_size).
+ * With aux_size == NULL the context's grow-only device cache supplies the
+ * memory (the reference's memcache_t, vk/context.hxx:110-134).
+ *
+ * All work is enqueued on the context's CUDA stream and returns without a
+ * host synchronisation (the reference records into a command buffer and runs
+ * on submit, src/vk/context.cxx:336-345).  Buffers are caller-owned device
+ * pointers.  Sorts are in place, as in the reference.  mgpu_synchronize()
+ * waits for the stream and reports device-side errors (a bounded look-back
+ * wait that gave up returns MGPU_ERR_LOOKBACK_TIMEOUT).  No entry point
+ * throws.  A context is used by one host thread at a time.
+ */
+#ifndef MGPU_GB300_H
+#define MGPU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MGPU_API __attribute__((visibility("default")))
+#else
+#define MGPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mgpu_status_t {
+  MGPU_OK = 0,
+  MGPU_ERR_INVALID_ARG = 1,      /* bad pointer, size, type or aux capacity */
+  MGPU_ERR_OOM = 2,              /* device allocation failed */
+  MGPU_ERR_LOOKBACK_TIMEOUT = 3, /* a bounded device-side wait gave up */
+  MGPU_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+  MGPU_ERR_UNSUPPORTED = 5,      /* type/size combination not built */
+  MGPU_ERR_BUDGET = 6,           /* serving: request exceeds the HBM budget */
+  MGPU_ERR_NOT_READY = 7         /* serving: request still in flight */
+} mgpu_status_t;
+
+/* Element types.  Codes are shared with the host oracle. */
+typedef enum mgpu_dtype_t {
+  MGPU_I32 = 0,
+  MGPU_U32 = 1,
+  MGPU_F32 = 2,
+  MGPU_I64 = 3,
+  MGPU_U64 = 4,
+  MGPU_F64 = 5
+} mgpu_dtype_t;
+
+/* Comparators of the merge family: std::less / std::greater. */
+typedef enum mgpu_comp_t { MGPU_LESS = 0, MGPU_GREATER = 1 } mgpu_comp_t;
+
+/* Scan/reduce operators (reference: op_t template argument, vk/scan.hxx:10-13). */
+typedef enum mgpu_op_t { MGPU_PLUS = 0, MGPU_MAX = 1, MGPU_MIN = 2 } mgpu_op_t;
+
+/* scan_type_t (reference: common/cta_scan.hxx:63-66). */
+typedef enum mgpu_scan_type_t { MGPU_SCAN_EXC = 0, MGPU_SCAN_INC = 1 } mgpu_scan_type_t;
+
+typedef struct mgpu_context mgpu_context_t;
+
+/* ---- context (replaces context_t / cmd_buffer_t / memcache_t,
+ *      vk/context.hxx:11-134, src/vk/context.cxx:15-439) ---- */
+
+/* Creates a context on `device`.  `stream` is a cudaStream_t to enqueue on,
+ * or NULL for a stream the context creates and owns. */
+MGPU_API mgpu_status_t mgpu_context_create(int device, void* stream, mgpu_context_t** out);
+MGPU_API mgpu_status_t mgpu_context_destroy(mgpu_context_t* ctx);
+/* Redirects later work to another cudaStream_t (NULL: the owned stream). */
+MGPU_API mgpu_status_t mgpu_context_set_stream(mgpu_context_t* ctx, void* stream);
+MGPU_API void* mgpu_context_stream(mgpu_context_t* ctx);
+/* Waits for the stream; returns the first device-side error since the last
+ * call (and clears it), or MGPU_ERR_CUDA. */
+MGPU_API mgpu_status_t mgpu_synchronize(mgpu_context_t* ctx);
+MGPU_API const char* mgpu_status_string(mgpu_status_t status);
+/* Text of the last CUDA error seen by this context. */
+MGPU_API const char* mgpu_last_error(mgpu_context_t* ctx);
+MGPU_API int mgpu_sm_count(mgpu_context_t* ctx);
+
+/* Device/host memory (context_t::alloc_gpu / alloc_cpu / free,
+ * src/vk/context.cxx:156-212) and stream-ordered copies
+ * (context_t::memcpy, :225-243; cmd_buffer_t::memcpy, :400-402). */
+MGPU_API mgpu_status_t mgpu_alloc_gpu(mgpu_context_t* ctx, size_t bytes, void** out);
+MGPU_API mgpu_status_t mgpu_alloc_cpu(mgpu_context_t* ctx, size_t bytes, void** out);
+MGPU_API mgpu_status_t mgpu_free(mgpu_context_t* ctx, void* p);
+MGPU_API mgpu_status_t mgpu_memcpy(mgpu_context_t* ctx, void* dest, const void* src, size_t bytes);
+MGPU_API mgpu_status_t mgpu_memset(mgpu_context_t* ctx, void* dest, int value, size_t bytes);
+
+/* ---- radix sort (vk::radix_sort, vk/radix.hxx:195-470) ----
+ * Stable LSD sort of `keys` in place by radix_permute_t order
+ * (common/cta_radix.hxx:6-64): unsigned keys by value, signed keys by value,
+ * float keys by bit order (-0.0 before +0.0, NaNs by bit pattern).  Values of
+ * `val_bytes` bytes (0 = keys only, 4, or 8) travel with their keys; the
+ * reference sorts keys only.  Keys: I32, U32, F32, I64, U64, F64.
+ * count < 2^30. */
+MGPU_API mgpu_status_t mgpu_radix_sort(mgpu_context_t* ctx, mgpu_dtype_t key_type, void* keys,
+  int val_bytes, void* vals, int64_t count, void* aux_data, size_t* aux_size);
+
+/* ---- merge (vk::merge key-value and keys-only, vk/merge.hxx:12-59) ----
+ * Stable merge of sorted A and B into C (ties take A first, bounds_lower,
+ * common/cta_merge.hxx:23-25).  vals may be NULL with val_bytes 0. */
+MGPU_API mgpu_status_t mgpu_merge(mgpu_context_t* ctx, mgpu_dtype_t key_type,
+  const void* a_keys, const void* a_vals, int64_t a_count,
+  const void* b_keys, const void* b_vals, int64_t b_count,
+  void* c_keys, void* c_vals, int val_bytes, mgpu_comp_t comp,
+  void* aux_data, size_t* aux_size);
+
+/* ---- mergesort (vk::mergesort_kv / mergesort_keys, vk/mergesort.hxx:10-93) ----
+ * Stable comparison sort in place.  vals may be NULL with val_bytes 0. */
+MGPU_API mgpu_status_t mgpu_mergesort(mgpu_context_t* ctx, mgpu_dtype_t key_type, void* keys,
+  int val_bytes, void* vals, int64_t count, mgpu_comp_t comp,
+  void* aux_data, size_t* aux_size);
+
+/* vk::mergesort_indices (vk/mergesort.hxx:95-103): sorts keys in place and
+ * writes each key's original index into `indices` (int32). */
+MGPU_API mgpu_status_t mgpu_mergesort_indices(mgpu_context_t* ctx, mgpu_dtype_t key_type,
+  void* keys, int32_t* indices, int64_t count, mgpu_comp_t comp,
+  void* aux_data, size_t* aux_size);
+
+/* ---- scan (vk::scan, vk/scan.hxx:10-115) ----
+ * out[i] = init (+) in[0] (+) ... (+) in[i-1]   (MGPU_SCAN_EXC)
+ * out[i] = init (+) in[0] (+) ... (+) in[i]     (MGPU_SCAN_INC)
+ * `init` is a host pointer to one element (NULL: the operator's identity).
+ * in == out scans in place, as the reference does.  `reduction`, if not
+ * NULL, is a device pointer that receives init (+) all inputs.
+ * Integer sums wrap in two's complement. */
+MGPU_API mgpu_status_t mgpu_scan(mgpu_context_t* ctx, mgpu_dtype_t type, mgpu_scan_type_t scan_type,
+  mgpu_op_t op, const void* in, void* out, int64_t count, const void* init,
+  void* reduction, void* aux_data, size_t* aux_size);
+
+/* ---- reduce (cta_reduce_t, common/cta_scan.hxx:9-59, as a device-wide
+ * primitive).  Writes init (+) all inputs to the device pointer `out`. */
+MGPU_API mgpu_status_t mgpu_reduce(mgpu_context_t* ctx, mgpu_dtype_t type, mgpu_op_t op,
+  const void* in, int64_t count, const void* init, void* out,
+  void* aux_data, size_t* aux_size);
+
+/* ---- transform (vk::transform / vk::launch, vk/transform.hxx:9-36) ----
+ * The generic form takes a C++ device lambda (mgpu::gb300::transform in the
+ * C++ headers).  The C ABI carries the element-wise operations of the
+ * reference's transform example (examples/vk_transform/vk_transform.cxx:
+ * 36-63) for callers without a CUDA compiler. */
+/* out[i] = start + i * step, for an element type of the table above. */
+MGPU_API mgpu_status_t mgpu_transform_iota(mgpu_context_t* ctx, mgpu_dtype_t type, void* out,
+  int64_t count, double start, double step);
+/* out[i] = value. */
+MGPU_API mgpu_status_t mgpu_transform_fill(mgpu_context_t* ctx, mgpu_dtype_t type, void* out,
+  int64_t count, double value);
+/* y[i] += a * x[i] (float32). */
+MGPU_API mgpu_status_t mgpu_transform_saxpy_f32(mgpu_context_t* ctx, float a, const float* x,
+  float* y, int64_t count);
+
+/* ---- segmented primitives (no reference counterpart: batched sort/scan
+ * over CSR segments, one launch sequence for all segments) ----
+ * `offsets` is a device array of num_segments + 1 int64 begin offsets;
+ * segment s is [offsets[s], offsets[s+1]).  Keys are sorted in radix order
+ * (as mgpu_radix_sort) within each segment; vals follow. */
+MGPU_API mgpu_status_t mgpu_segmented_sort(mgpu_context_t* ctx, mgpu_dtype_t key_type, void* keys,
+  int val_bytes, void* vals, int64_t count, const int64_t* offsets,
+  int64_t num_segments, void* aux_data, size_t* aux_size);
+/* Scan restarted at every segment head with `init`. */
+MGPU_API mgpu_status_t mgpu_segmented_scan(mgpu_context_t* ctx, mgpu_dtype_t type,
+  mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,
+  const int64_t* offsets, int64_t num_segments, const void* init,
+  void* aux_data, size_t* aux_size);
+
+/* ---- launch profiling (no reference counterpart; the reference times
+ * whole command buffers with clock_gettime, examples/vk_radix/vk_radix.cxx:
+ * 51-63).  When enabled, every kernel the library launches on this context
+ * is bracketed by CUDA events on its stream. */
+MGPU_API mgpu_status_t mgpu_profile_enable(mgpu_context_t* ctx, int enable);
+/* Synchronises, then returns per-kernel launch counts and total device
+ * milliseconds; names are written as a '\n'-separated list into `names`.
+ * Clears the record.  Returns the number of kernels in *num (≤ capacity). */
+MGPU_API mgpu_status_t mgpu_profile_read(mgpu_context_t* ctx, char* names, size_t names_bytes,
+  int64_t* launches, double* total_ms, int capacity, int* num);
+/* Kernel launches issued on this context since creation. */
+MGPU_API int64_t mgpu_launch_count(mgpu_context_t* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MGPU_GB300_H */

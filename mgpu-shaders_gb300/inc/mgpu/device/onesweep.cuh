@@ -1,0 +1,320 @@
+// LSD radix sort for sm_103a: one histogram kernel for all digit places, then
+// one single-pass "onesweep" scatter kernel per 8-bit digit.
+//
+// Reference behaviour (seanbaxter/mgpu-shaders): vk::radix_sort
+// (vk/radix.hxx:195-470) runs, per digit, an upsweep histogram, a scan of
+// the per-tile counts (radix_scan_8, :13-185) and a downsweep that ranks the
+// digits with warp ballots (cta_radix_rank_t<..., radix_kind_ballot>,
+// common/cta_radix.hxx:212-351) and scatters through shared memory.  The
+// result is a stable LSD sort over radix_permute_t bits.  This file computes
+// the same permutation with a different schedule:
+//
+//  * radix_histogram: every digit place's 256-bin histogram from a single
+//    read of the keys (4 B/key instead of one upsweep read per digit).
+//  * onesweep_pass: one launch per digit.  Each CTA takes the next tile id
+//    from an atomic counter (so every predecessor tile is already resident),
+//    bulk-copies its keys and values into shared memory with the TMA engine,
+//    ranks digits per warp with match.any (stable: rows of 32 lanes in
+//    element order), publishes its per-digit counts, then walks back over
+//    predecessor tiles' published counts (decoupled look-back) to find its
+//    global offset per digit.  Keys and values are scattered to shared memory
+//    in local digit order and written out in runs, so global stores coalesce.
+//    Per pass the kernel reads and writes each key and value once.
+//
+// The look-back status of (tile, digit) is one 32-bit word: two flag bits
+// (aggregate / inclusive prefix) over a 30-bit count, hence count < 2^30.
+#pragma once
+
+#include "common.cuh"
+#include <type_traits>
+
+namespace mgpu {
+namespace device {
+
+// Value type of a keys-only sort.
+struct no_values {};
+
+constexpr int radix_bins = 256;
+constexpr uint32_t lb_agg = 1u << 30;
+constexpr uint32_t lb_inc = 2u << 30;
+constexpr uint32_t lb_count = (1u << 30) - 1;
+
+template<typename K, typename V>
+struct onesweep_args {
+  typedef typename radix_key<K>::bits_t U;
+  const U* keys_in;          // K on the first pass, radix bits after
+  U* keys_out;               // radix bits, or K on the last pass
+  const V* vals_in;
+  V* vals_out;
+  int64_t count;
+  int shift;                 // bit offset of this pass's digit
+  const uint32_t* hist;      // this pass's 256 global digit counts
+  uint32_t* lookback;        // this pass's [num_tiles][256] status words
+  uint32_t* tile_counter;    // this pass's dynamic tile counter
+  int* error;
+  int first;                 // convert K -> bits on load
+  int last;                  // convert bits -> K on store
+  int tma;                   // pointers allow 16-byte bulk copies
+};
+
+template<typename K, typename V, int NT, int ITEMS>
+struct onesweep_layout {
+  typedef typename radix_key<K>::bits_t U;
+  static constexpr bool has_values = !std::is_same<V, no_values>::value;
+  static constexpr int tile = NT * ITEMS;
+  static constexpr int num_warps = NT / 32;
+  static constexpr size_t keys_off = 0;
+  static constexpr size_t vals_off = keys_off + sizeof(U) * tile;
+  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
+  static constexpr size_t gbase_off = hist_off + sizeof(uint32_t) * num_warps * radix_bins;
+  static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
+  static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
+  static constexpr size_t tile_off = bar_off + sizeof(uint64_t) * 2;
+  static constexpr size_t bytes = tile_off + 16;
+  static_assert(NT >= radix_bins && NT % 32 == 0, "one thread per digit");
+  static_assert((sizeof(U) * tile) % 16 == 0, "bulk-copy granularity");
+};
+
+// Exclusive scan of two 256-entry arrays held by threads 0..255 (one digit
+// each).  Every thread of the CTA must call it.
+__device__ __forceinline__ void scan_256_pair(uint32_t& x, uint32_t& y, uint32_t* tmp) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t xi = x, yi = y;
+#pragma unroll
+  for(int off = 1; off < 32; off <<= 1) {
+    uint32_t tx = __shfl_up_sync(0xffffffffu, xi, off);
+    uint32_t ty = __shfl_up_sync(0xffffffffu, yi, off);
+    if(lane >= off) { xi += tx; yi += ty; }
+  }
+  if(tid < radix_bins && lane == 31) { tmp[warp] = xi; tmp[8 + warp] = yi; }
+  __syncthreads();
+  if(tid < radix_bins) {
+    uint32_t px = 0, py = 0;
+    for(int w = 0; w < warp; ++w) { px += tmp[w]; py += tmp[8 + w]; }
+    x = px + xi - x;
+    y = py + yi - y;
+  }
+}
+
+// Histogram of every digit place in one read.  Also clears the look-back
+// status words of all passes (zero_words uint4s), which must be zero before
+// the first scatter pass starts.
+template<typename K, int NT, int PASSES>
+__global__ void __launch_bounds__(NT)
+radix_histogram(const K* keys, int64_t count, uint32_t* hist, uint4* zero, int64_t zero_vec4,
+  int vectorised) {
+  typedef typename radix_key<K>::bits_t U;
+  __shared__ uint32_t sh[PASSES * radix_bins];
+  const int tid = threadIdx.x;
+  for(int i = tid; i < PASSES * radix_bins; i += NT) sh[i] = 0;
+  const int64_t gid = (int64_t)blockIdx.x * NT + tid;
+  const int64_t stride = (int64_t)gridDim.x * NT;
+  for(int64_t i = gid; i < zero_vec4; i += stride) zero[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+
+  auto count_key = [&](K key) {
+    U u = radix_key<K>::to_bits(key);
+#pragma unroll
+    for(int p = 0; p < PASSES; ++p)
+      atomicAdd(&sh[p * radix_bins + extract_digit(u, 8 * p, 8)], 1u);
+  };
+  constexpr int per_vec = 16 / sizeof(K);
+  int64_t num_vec = vectorised ? count / per_vec : 0;
+  const uint4* kv = (const uint4*)keys;
+  for(int64_t i = gid; i < num_vec; i += stride) {
+    uint4 v = kv[i];
+    const K* e = (const K*)&v;
+#pragma unroll
+    for(int j = 0; j < per_vec; ++j) count_key(e[j]);
+  }
+  for(int64_t i = num_vec * per_vec + gid; i < count; i += stride) count_key(keys[i]);
+  __syncthreads();
+  for(int i = tid; i < PASSES * radix_bins; i += NT)
+    if(sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS>
+__global__ void __launch_bounds__(NT, MIN_BLOCKS)
+onesweep_pass(onesweep_args<K, V> a) {
+  typedef onesweep_layout<K, V, NT, ITEMS> L;
+  typedef typename L::U U;
+  constexpr int TILE = L::tile;
+  constexpr int NWARPS = L::num_warps;
+  constexpr bool HAS_V = L::has_values;
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  U* ks = (U*)(smem + L::keys_off);
+  V* vs = (V*)(smem + L::vals_off);
+  uint32_t* whist = (uint32_t*)(smem + L::hist_off);
+  int* gbase = (int*)(smem + L::gbase_off);
+  uint32_t* stmp = (uint32_t*)(smem + L::scan_off);
+  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
+  int* s_tile = (int*)(smem + L::tile_off);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if(tid == 0) {
+    *s_tile = (int)atomicAdd(a.tile_counter, 1u);
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  for(int i = tid; i < NWARPS * radix_bins; i += NT) whist[i] = 0;
+  __syncthreads();
+
+  const int tile = *s_tile;
+  const int64_t base = (int64_t)tile * TILE;
+  const int valid = (int)min((int64_t)TILE, a.count - base);
+  const bool bulk = a.tma && valid == TILE;
+
+  if(bulk && tid == 0) {
+    constexpr uint32_t kbytes = sizeof(U) * TILE;
+    constexpr uint32_t vbytes = HAS_V ? sizeof(V) * TILE : 0;
+    mbar_arrive_expect_tx(bar, kbytes + vbytes);
+    bulk_load(ks, a.keys_in + base, kbytes, bar);
+    if(HAS_V) bulk_load(vs, a.vals_in + base, vbytes, bar);
+  }
+
+  // Element e of item i in this thread: warp-contiguous rows of 32 lanes,
+  // e = warp_base + 32 * i + lane; it is in range while 32 * i < rem.
+  const int warp_base = warp * 32 * ITEMS;
+  const int rem = valid - warp_base - lane;
+  U k[ITEMS];
+  if(bulk) {
+    bool ok = mbar_wait_bounded(bar, 0, a.error);
+    if(__syncthreads_or(!ok)) {
+      // The copy did not complete in time: wait once more (bounded) so no
+      // bulk copy is still writing this CTA's shared memory, then leave.
+      mbar_wait_bounded(bar, 0, a.error);
+      return;
+    }
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) k[i] = ks[warp_base + 32 * i + lane];
+  } else {
+    const U* src = a.keys_in + base + warp_base + lane;
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) k[i] = 32 * i < rem ? src[32 * i] : ~(U)0;
+  }
+  if(a.first) {
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      if(32 * i < rem) {
+        K key;
+        memcpy(&key, &k[i], sizeof(K));
+        k[i] = radix_key<K>::to_bits(key);
+      }
+    }
+  }
+
+  // Warp-level stable ranking: item i of every lane forms one row; lanes
+  // holding equal digits are peers.  The rank counts earlier rows and lower
+  // lanes of the same row (element order), via a per-warp digit counter.
+  uint32_t r[ITEMS];
+  uint32_t* wh = whist + warp * radix_bins;
+  const uint32_t lt_mask = lanemask_lt();
+#pragma unroll
+  for(int i = 0; i < ITEMS; ++i) {
+    uint32_t d = extract_digit(k[i], a.shift, 8);
+    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t below = peers & lt_mask;
+    uint32_t cnt = wh[d];
+    __syncwarp();
+    if(!below) wh[d] = cnt + __popc(peers);
+    __syncwarp();
+    r[i] = cnt + __popc(below);
+  }
+  __syncthreads();
+
+  // Digit `tid`: counts per warp -> exclusive offsets over warps; publish the
+  // tile's count (inclusive for tile 0) before scanning, so successors can
+  // proceed as early as possible.
+  uint32_t tile_cnt = 0, glob_cnt = 0, valid_cnt = 0;
+  if(tid < radix_bins) {
+#pragma unroll 4
+    for(int w = 0; w < NWARPS; ++w) {
+      uint32_t c = whist[w * radix_bins + tid];
+      whist[w * radix_bins + tid] = tile_cnt;
+      tile_cnt += c;
+    }
+    valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
+    st_relaxed(&a.lookback[(int64_t)tile * radix_bins + tid],
+      (tile ? lb_agg : lb_inc) | valid_cnt);
+    glob_cnt = a.hist[tid];
+  }
+  uint32_t tile_start = tile_cnt, glob_start = glob_cnt;
+  scan_256_pair(tile_start, glob_start, stmp);
+
+  if(tid < radix_bins) {
+    uint32_t excl = 0;
+    if(tile > 0) {
+      int j = tile - 1;
+      int spins = 0;
+      while(true) {
+        uint32_t s = ld_relaxed(&a.lookback[(int64_t)j * radix_bins + tid]);
+        uint32_t flag = s & ~lb_count;
+        if(!flag) {
+          ++spins;
+          if(spins >= spin_limit ||
+             (0 == (spins & (spin_poll_error - 1)) && error_raised(a.error))) {
+            raise_error(a.error, err_lookback_timeout);
+            break;
+          }
+          continue;
+        }
+        excl += s & lb_count;
+        if(flag == lb_inc) break;
+        --j;
+      }
+      st_relaxed(&a.lookback[(int64_t)tile * radix_bins + tid], lb_inc | (excl + valid_cnt));
+    }
+    gbase[tid] = (int)(glob_start + excl - tile_start);
+#pragma unroll 4
+    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] += tile_start;
+  }
+  __syncthreads();
+
+  // Local positions; scatter keys (and values) into shared memory in digit
+  // order.  All reads of the staged keys happened before the barriers above.
+#pragma unroll
+  for(int i = 0; i < ITEMS; ++i) {
+    uint32_t d = extract_digit(k[i], a.shift, 8);
+    r[i] += wh[d];
+    ks[r[i]] = k[i];
+  }
+  if constexpr(HAS_V) {
+    V v[ITEMS];
+    if(bulk) {
+#pragma unroll
+      for(int i = 0; i < ITEMS; ++i) v[i] = vs[warp_base + 32 * i + lane];
+    } else {
+      const V* src = a.vals_in + base + warp_base + lane;
+#pragma unroll
+      for(int i = 0; i < ITEMS; ++i) v[i] = 32 * i < rem ? src[32 * i] : V();
+    }
+    __syncthreads();
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) vs[r[i]] = v[i];
+  }
+  __syncthreads();
+
+  // Write out in local order: consecutive threads hit consecutive addresses
+  // inside each digit's run.
+  const int out_rem = valid - tid;
+#pragma unroll
+  for(int j = 0; j < ITEMS; ++j) {
+    int idx = j * NT + tid;
+    if(j * NT < out_rem) {
+      U u = ks[idx];
+      uint32_t d = extract_digit(u, a.shift, 8);
+      uint32_t dst = (uint32_t)gbase[d] + idx;
+      if(a.last) {
+        K key = radix_key<K>::from_bits(u);
+        memcpy(&a.keys_out[dst], &key, sizeof(K));
+      } else {
+        a.keys_out[dst] = u;
+      }
+      if constexpr(HAS_V) a.vals_out[dst] = vs[idx];
+    }
+  }
+}
+
+}  // namespace device
+}  // namespace mgpu

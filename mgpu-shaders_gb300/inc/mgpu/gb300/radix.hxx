@@ -1,0 +1,151 @@
+// mgpu::gb300::radix_sort - the host driver of the onesweep LSD radix sort.
+//
+// Drop-in for vk::radix_sort (vk/radix.hxx:195-470): same two-phase aux
+// protocol (a call with aux_data == nullptr only adds to aux_size), in-place
+// result in `keys`, and the same key order (radix_permute_t bits).  The
+// template knobs are (nt, vt) = (threads per CTA, keys per thread); the digit
+// width is 8 bits, the reference's benchmarked setting (radix_sort<256,16,8>,
+// examples/vk_radix/vk_radix.cxx:56).  Key-value sorting is an addition.
+//
+// Launch sequence per sort: one memset of the small header (histograms and
+// tile counters), radix_histogram (all digit places, also clears the
+// look-back words), then one onesweep_pass per digit, ping-ponging between
+// `keys`/`vals` and the aux copies.  The pass count is even for 4- and 8-byte
+// keys, so the result lands in the caller's buffers.  No host
+// synchronisation: the sequence is stream-ordered and graph-capturable.
+#pragma once
+
+#include "context.hxx"
+#include "../device/onesweep.cuh"
+
+namespace mgpu {
+namespace gb300 {
+
+// Default tile shapes per key width (threads, keys per thread, CTAs per SM).
+template<int key_bytes> struct radix_tuning;
+template<> struct radix_tuning<4> { enum { nt = 256, vt = 16, min_blocks = 3 }; };
+template<> struct radix_tuning<8> { enum { nt = 256, vt = 12, min_blocks = 3 }; };
+
+// Largest count the 30-bit look-back status word can carry.
+constexpr int64_t radix_max_count = (int64_t(1) << 30) - 1;
+
+template<
+  int nt = radix_tuning<sizeof(uint32_t)>::nt,
+  int vt = radix_tuning<sizeof(uint32_t)>::vt,
+  int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
+  typename K, typename V>
+status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys, V* vals,
+  int64_t count) {
+  using namespace device;
+  typedef typename radix_key<K>::bits_t U;
+  constexpr bool has_values = !std::is_same<V, no_values>::value;
+  constexpr int passes = (int)sizeof(K);          // 8-bit digits
+  constexpr int tile = nt * vt;
+  typedef onesweep_layout<K, V, nt, vt> L;
+
+  if(count < 0 || count > radix_max_count) return MGPU_ERR_INVALID_ARG;
+
+  int64_t num_tiles = div_up(count, tile);
+  aux_layout_t lay;
+  size_t header_off = lay.add(sizeof(uint32_t) * (passes * radix_bins + passes));
+  size_t header_bytes = lay.total;
+  size_t lookback_off = lay.add(sizeof(uint32_t) * radix_bins * passes * num_tiles);
+  size_t lookback_bytes = lay.total - lookback_off;
+  size_t keys_off = lay.add(sizeof(K) * count);
+  size_t vals_off = has_values ? lay.add(sizeof(V) * count) : 0;
+  (void)header_off;
+
+  char* base = nullptr;
+  status_t st;
+  if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
+  if(count == 0) return MGPU_OK;
+  if(!keys || (has_values && !vals)) return MGPU_ERR_INVALID_ARG;
+
+  uint32_t* hist = (uint32_t*)base;
+  uint32_t* counters = hist + passes * radix_bins;
+  uint32_t* lookback = (uint32_t*)(base + lookback_off);
+  U* alt_keys = (U*)(base + keys_off);
+  V* alt_vals = has_values ? (V*)(base + vals_off) : nullptr;
+
+  if(ctx.check(cudaMemsetAsync(base, 0, header_bytes, ctx.stream))) return MGPU_ERR_CUDA;
+
+  // Histogram of every digit place; also clears the look-back words.
+  {
+    constexpr int hnt = 512;
+    int64_t want = div_up(count, (int64_t)hnt * 16);
+    int grid = (int)std::min<int64_t>(std::max<int64_t>(want, 1), (int64_t)ctx.sm_count * 4);
+    int vec = aligned16_host(keys);
+    st = ctx.launch("radix_histogram", [&] {
+      radix_histogram<K, hnt, passes><<<grid, hnt, 0, ctx.stream>>>(keys, count, hist,
+        (uint4*)lookback, (int64_t)(lookback_bytes / 16), vec);
+    });
+    if(st) return st;
+  }
+
+  auto kernel = onesweep_pass<K, V, nt, vt, min_blocks>;
+  if(!ctx.allow_smem(kernel, L::bytes)) return MGPU_ERR_CUDA;
+
+  U* k_io[2] = { (U*)keys, alt_keys };
+  V* v_io[2] = { vals, alt_vals };
+  for(int p = 0; p < passes; ++p) {
+    onesweep_args<K, V> a;
+    a.keys_in = k_io[p & 1];
+    a.keys_out = k_io[(p + 1) & 1];
+    a.vals_in = v_io[p & 1];
+    a.vals_out = v_io[(p + 1) & 1];
+    a.count = count;
+    a.shift = 8 * p;
+    a.hist = hist + p * radix_bins;
+    a.lookback = lookback + (size_t)p * num_tiles * radix_bins;
+    a.tile_counter = counters + p;
+    a.error = ctx.d_error;
+    a.first = p == 0;
+    a.last = p == passes - 1;
+    a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));
+    st = ctx.launch("onesweep_pass", [&] {
+      kernel<<<(unsigned)num_tiles, nt, L::bytes, ctx.stream>>>(a);
+    });
+    if(st) return st;
+  }
+  static_assert(passes % 2 == 0, "result must land in the caller's buffers");
+  return MGPU_OK;
+}
+
+// Keys-only form (the reference's signature, vk/radix.hxx:197-198).
+template<
+  int nt = radix_tuning<sizeof(uint32_t)>::nt,
+  int vt = radix_tuning<sizeof(uint32_t)>::vt,
+  int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
+  typename K>
+status_t radix_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* keys, int64_t count) {
+  return radix_sort_kv<nt, vt, min_blocks>(aux_data, &aux_size, ctx, keys,
+    (device::no_values*)nullptr, count);
+}
+
+// Key-value form.
+template<
+  int nt = radix_tuning<sizeof(uint32_t)>::nt,
+  int vt = radix_tuning<sizeof(uint32_t)>::vt,
+  int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
+  typename K, typename V>
+status_t radix_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* keys, V* vals,
+  int64_t count) {
+  return radix_sort_kv<nt, vt, min_blocks>(aux_data, &aux_size, ctx, keys, vals, count);
+}
+
+// Memcache forms: aux comes from the context's grow-only cache.
+template<typename K>
+status_t radix_sort(context_t& ctx, K* keys, int64_t count) {
+  constexpr int b = sizeof(K);
+  return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
+    nullptr, nullptr, ctx, keys, (device::no_values*)nullptr, count);
+}
+template<typename K, typename V>
+status_t radix_sort(context_t& ctx, K* keys, V* vals, int64_t count) {
+  constexpr int b = sizeof(K);
+  return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
+    nullptr, nullptr, ctx, keys, vals, count);
+}
+
+}  // namespace gb300
+}  // namespace mgpu

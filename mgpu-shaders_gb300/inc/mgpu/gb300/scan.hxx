@@ -1,0 +1,105 @@
+// mgpu::gb300::scan / reduce - host drivers of the single-pass scan and the
+// single-launch reduce.
+//
+// Drop-in for vk::scan (vk/scan.hxx:10-115): in-place exclusive scan with
+// `init` and `op`, same two-phase aux protocol.  Additions: the scan type
+// template (scan_type_exc / scan_type_inc, the enum of
+// common/cta_scan.hxx:63-66), an out-of-place overload, an optional device
+// reduction output, and reduce().  `init` enters once, as the left-most
+// operand: exclusive out[0] = init; inclusive out[i] = init (+) in[0..i].
+#pragma once
+
+#include "context.hxx"
+#include "../device/scan.cuh"
+
+namespace mgpu {
+namespace gb300 {
+
+enum scan_type_t { scan_type_exc = 0, scan_type_inc = 1 };
+
+template<typename T> using plus_t = device::plus_t<T>;
+template<typename T> using maximum_t = device::max_t<T>;
+template<typename T> using minimum_t = device::min_t<T>;
+
+template<int bytes> struct scan_tuning;
+template<> struct scan_tuning<4> { enum { nt = 256, vt = 16 }; };
+template<> struct scan_tuning<8> { enum { nt = 256, vt = 8 }; };
+
+template<scan_type_t scan_type = scan_type_exc,
+  int nt = 0, int vt = 0, typename T, typename op_t = plus_t<T>>
+status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
+  T* out, T init = op_t::identity(), op_t op = op_t(), T* reduction = nullptr) {
+  using namespace device;
+  constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
+  constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
+  constexpr int tile = NT * VT;
+  if(count < 0) return MGPU_ERR_INVALID_ARG;
+  int64_t num_tiles = div_up(count, tile);
+  if(num_tiles > 0xffffffffll) return MGPU_ERR_INVALID_ARG;
+  aux_layout_t lay;
+  lay.add(16);                                     // tile counter
+  size_t status_off = lay.add(tile_status_t<T>::bytes(num_tiles));
+  char* base = nullptr;
+  status_t st;
+  if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
+  if(count == 0) {
+    if(reduction && ctx.check(cudaMemcpyAsync(reduction, &init, sizeof(T),
+      cudaMemcpyHostToDevice, ctx.stream))) return MGPU_ERR_CUDA;
+    if(reduction && ctx.check(cudaStreamSynchronize(ctx.stream))) return MGPU_ERR_CUDA;
+    return MGPU_OK;
+  }
+  if(!in || !out) return MGPU_ERR_INVALID_ARG;
+  if(ctx.check(cudaMemsetAsync(base, 0, lay.total, ctx.stream))) return MGPU_ERR_CUDA;
+  tile_status_t<T> status;
+  status.bind(base + status_off, num_tiles);
+  int vec = aligned16_host(in) && aligned16_host(out);
+  return ctx.launch(scan_type == scan_type_exc ? "scan_exc" : "scan_inc", [&] {
+    scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc>
+      <<<(unsigned)num_tiles, NT, 0, ctx.stream>>>(in, out, count, init, op, status,
+        (uint32_t*)base, reduction, ctx.d_error, vec);
+  });
+}
+
+// The reference's in-place form: scan(aux_data, aux_size, cmd, data, count,
+// init, op) is exclusive (vk/scan.hxx:12-13).
+template<scan_type_t scan_type = scan_type_exc, int nt = 0, int vt = 0, typename T,
+  typename op_t = plus_t<T>>
+status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t count,
+  T init = op_t::identity(), op_t op = op_t()) {
+  return scan<scan_type, nt, vt>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
+}
+
+// Memcache form.
+template<scan_type_t scan_type = scan_type_exc, typename T, typename op_t = plus_t<T>>
+status_t scan(context_t& ctx, const T* in, int64_t count, T* out, T init = op_t::identity(),
+  op_t op = op_t(), T* reduction = nullptr) {
+  return scan<scan_type>(nullptr, (size_t*)nullptr, ctx, in, count, out, init, op, reduction);
+}
+
+template<int nt = 0, int vt = 0, typename T, typename op_t = plus_t<T>>
+status_t reduce(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
+  T* out, T init = op_t::identity(), op_t op = op_t()) {
+  using namespace device;
+  constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
+  constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
+  constexpr int tile = NT * VT;
+  if(count < 0) return MGPU_ERR_INVALID_ARG;
+  int64_t num_tiles = div_up(count, tile);
+  int grid = (int)std::min<int64_t>(std::max<int64_t>(num_tiles, 1), (int64_t)ctx.sm_count * 8);
+  aux_layout_t lay;
+  lay.add(16);
+  size_t part_off = lay.add(sizeof(T) * grid);
+  char* base = nullptr;
+  status_t st;
+  if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
+  if(!out || (count > 0 && !in)) return MGPU_ERR_INVALID_ARG;
+  if(ctx.check(cudaMemsetAsync(base, 0, 16, ctx.stream))) return MGPU_ERR_CUDA;
+  int vec = aligned16_host(in);
+  return ctx.launch("reduce", [&] {
+    reduce_kernel<T, op_t, NT, VT><<<grid, NT, 0, ctx.stream>>>(in, count, init, op,
+      (T*)(base + part_off), (uint32_t*)base, out, vec);
+  });
+}
+
+}  // namespace gb300
+}  // namespace mgpu

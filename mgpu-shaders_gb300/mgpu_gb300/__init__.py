@@ -1,0 +1,236 @@
+"""Python access to libmgpu_gb300.so through its C ABI (include/mgpu_gb300.h).
+
+This is a thin ctypes layer for tests, benchmarks and Python callers.  Device
+memory comes from torch (plumbing only); every computation runs in the CUDA
+kernels of libmgpu_gb300.so.  There is no CPU fallback: if the library is
+missing or fails to load, import of the library raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import MgpuError, lib, library_path  # noqa: F401
+
+DTYPES = {
+    np.dtype(np.int32): 0,
+    np.dtype(np.uint32): 1,
+    np.dtype(np.float32): 2,
+    np.dtype(np.int64): 3,
+    np.dtype(np.uint64): 4,
+    np.dtype(np.float64): 5,
+}
+SCAN_TYPES = {"exc": 0, "inc": 1}
+OPS = {"plus": 0, "max": 1, "min": 2}
+COMPS = {"less": 0, "greater": 1}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class DeviceArray:
+    """A device buffer of `count` elements of a numpy dtype, held by a torch
+    uint8 tensor.  Only its pointer is handed to the library."""
+
+    def __init__(self, count, dtype, tensor=None):
+        torch = _torch()
+        self.dtype = np.dtype(dtype)
+        self.count = int(count)
+        nbytes = max(1, self.count * self.dtype.itemsize)
+        self.tensor = tensor if tensor is not None else torch.empty(
+            nbytes, dtype=torch.uint8, device="cuda")
+
+    @classmethod
+    def from_numpy(cls, arr, stream=None):
+        torch = _torch()
+        arr = np.ascontiguousarray(arr)
+        out = cls(arr.size, arr.dtype)
+        if arr.size:
+            host = torch.from_numpy(arr.view(np.uint8).reshape(-1))
+            out.tensor[: host.numel()].copy_(host, non_blocking=False)
+        return out
+
+    @property
+    def ptr(self):
+        return self.tensor.data_ptr()
+
+    @property
+    def nbytes(self):
+        return self.count * self.dtype.itemsize
+
+    def numpy(self):
+        if self.count == 0:
+            return np.empty(0, self.dtype)
+        host = self.tensor[: self.nbytes].cpu().numpy()
+        return host.view(self.dtype).copy()
+
+    def copy_from(self, other):
+        self.tensor[: self.nbytes].copy_(other.tensor[: other.nbytes])
+
+
+class Context:
+    """mgpu_context_t on one device, enqueuing on torch's current stream of
+    that device unless `stream` (a cudaStream_t handle) is given."""
+
+    def __init__(self, device=0, stream=None, use_torch_stream=True):
+        torch = _torch()
+        if stream is None and use_torch_stream:
+            stream = torch.cuda.current_stream(device).cuda_stream
+        self._h = ctypes.c_void_p()
+        _lib.check(lib().mgpu_context_create(device, ctypes.c_void_p(stream), ctypes.byref(self._h)),
+                   None)
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().mgpu_context_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        _lib.check(rc, self._h)
+
+    def synchronize(self):
+        self._check(lib().mgpu_synchronize(self._h))
+
+    def set_stream(self, stream):
+        self._check(lib().mgpu_context_set_stream(self._h, ctypes.c_void_p(stream)))
+
+    @property
+    def sm_count(self):
+        return lib().mgpu_sm_count(self._h)
+
+    @property
+    def launch_count(self):
+        return lib().mgpu_launch_count(self._h)
+
+    # --- profiling ---
+    def profile(self, enable=True):
+        self._check(lib().mgpu_profile_enable(self._h, int(bool(enable))))
+
+    def profile_read(self):
+        cap = 64
+        names = ctypes.create_string_buffer(8192)
+        launches = (ctypes.c_int64 * cap)()
+        total = (ctypes.c_double * cap)()
+        num = ctypes.c_int()
+        self._check(lib().mgpu_profile_read(self._h, names, 8192, launches, total, cap,
+                                            ctypes.byref(num)))
+        keys = names.value.decode().split("\n")
+        return {keys[i]: (launches[i], total[i]) for i in range(num.value)}
+
+    # --- aux sizing helper: two-phase protocol ---
+    @staticmethod
+    def _aux_args(aux):
+        if aux is None:
+            return None, None
+        ptr, size = aux
+        return ctypes.c_void_p(ptr), ctypes.byref(ctypes.c_size_t(size))
+
+    # --- primitives ---
+    def radix_sort_aux_size(self, key_dtype, val_dtype, count):
+        size = ctypes.c_size_t(0)
+        self._check(lib().mgpu_radix_sort(self._h, DTYPES[np.dtype(key_dtype)], None,
+                                          0 if val_dtype is None else np.dtype(val_dtype).itemsize,
+                                          None, count, None, ctypes.byref(size)))
+        return size.value
+
+    def radix_sort(self, keys, vals=None, aux=None):
+        """In-place stable radix sort of DeviceArray keys (and vals)."""
+        a, s = self._aux_args(aux)
+        self._check(lib().mgpu_radix_sort(
+            self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr),
+            0 if vals is None else vals.dtype.itemsize,
+            None if vals is None else ctypes.c_void_p(vals.ptr), keys.count, a, s))
+
+    def merge(self, a_keys, a_vals, b_keys, b_vals, c_keys, c_vals, comp="less", aux=None):
+        a, s = self._aux_args(aux)
+        vb = 0 if a_vals is None else a_vals.dtype.itemsize
+        vp = (lambda x: None if x is None else ctypes.c_void_p(x.ptr))
+        self._check(lib().mgpu_merge(
+            self._h, DTYPES[a_keys.dtype], vp(a_keys), vp(a_vals), a_keys.count,
+            vp(b_keys), vp(b_vals), b_keys.count, vp(c_keys), vp(c_vals), vb, COMPS[comp], a, s))
+
+    def mergesort(self, keys, vals=None, comp="less", aux=None):
+        a, s = self._aux_args(aux)
+        self._check(lib().mgpu_mergesort(
+            self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr),
+            0 if vals is None else vals.dtype.itemsize,
+            None if vals is None else ctypes.c_void_p(vals.ptr), keys.count, COMPS[comp], a, s))
+
+    def mergesort_indices(self, keys, indices, comp="less", aux=None):
+        a, s = self._aux_args(aux)
+        self._check(lib().mgpu_mergesort_indices(
+            self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr), ctypes.c_void_p(indices.ptr),
+            keys.count, COMPS[comp], a, s))
+
+    def scan(self, data_in, data_out, scan_type="exc", op="plus", init=None, reduction=None,
+             aux=None):
+        a, s = self._aux_args(aux)
+        init_p = None
+        if init is not None:
+            init_arr = np.array([init], dtype=data_in.dtype)
+            init_p = init_arr.ctypes.data_as(ctypes.c_void_p)
+        self._check(lib().mgpu_scan(
+            self._h, DTYPES[data_in.dtype], SCAN_TYPES[scan_type], OPS[op],
+            ctypes.c_void_p(data_in.ptr), ctypes.c_void_p(data_out.ptr), data_in.count, init_p,
+            None if reduction is None else ctypes.c_void_p(reduction.ptr), a, s))
+
+    def reduce(self, data_in, out, op="plus", init=None, aux=None):
+        a, s = self._aux_args(aux)
+        init_p = None
+        if init is not None:
+            init_arr = np.array([init], dtype=data_in.dtype)
+            init_p = init_arr.ctypes.data_as(ctypes.c_void_p)
+        self._check(lib().mgpu_reduce(
+            self._h, DTYPES[data_in.dtype], OPS[op], ctypes.c_void_p(data_in.ptr), data_in.count,
+            init_p, ctypes.c_void_p(out.ptr), a, s))
+
+    def segmented_sort(self, keys, vals, offsets, aux=None):
+        a, s = self._aux_args(aux)
+        self._check(lib().mgpu_segmented_sort(
+            self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr),
+            0 if vals is None else vals.dtype.itemsize,
+            None if vals is None else ctypes.c_void_p(vals.ptr), keys.count,
+            ctypes.c_void_p(offsets.ptr), offsets.count - 1, a, s))
+
+    def segmented_scan(self, data_in, data_out, offsets, scan_type="inc", op="plus", init=None,
+                       aux=None):
+        a, s = self._aux_args(aux)
+        init_p = None
+        if init is not None:
+            init_arr = np.array([init], dtype=data_in.dtype)
+            init_p = init_arr.ctypes.data_as(ctypes.c_void_p)
+        self._check(lib().mgpu_segmented_scan(
+            self._h, DTYPES[data_in.dtype], SCAN_TYPES[scan_type], OPS[op],
+            ctypes.c_void_p(data_in.ptr), ctypes.c_void_p(data_out.ptr), data_in.count,
+            ctypes.c_void_p(offsets.ptr), offsets.count - 1, init_p, a, s))
+
+    def transform_iota(self, out, start=0.0, step=1.0):
+        self._check(lib().mgpu_transform_iota(self._h, DTYPES[out.dtype], ctypes.c_void_p(out.ptr),
+                                              out.count, float(start), float(step)))
+
+    def transform_fill(self, out, value):
+        self._check(lib().mgpu_transform_fill(self._h, DTYPES[out.dtype], ctypes.c_void_p(out.ptr),
+                                              out.count, float(value)))
+
+    def transform_saxpy(self, a, x, y):
+        self._check(lib().mgpu_transform_saxpy_f32(self._h, ctypes.c_float(a),
+                                                   ctypes.c_void_p(x.ptr), ctypes.c_void_p(y.ptr),
+                                                   x.count))
+
+
+def build_dir():
+    return os.path.dirname(library_path())
