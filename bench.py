@@ -4,11 +4,11 @@ uint32 values (uniform 32-bit keys, values = index) on one GB300.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 One step = one in-place radix sort of 2^28 key/value pairs through the C ABI
-(mgpu_radix_sort).  Every timed step sorts its own unsorted copy of the input,
-prepared before the timed region, so no restore copy is timed; each copy is
-2 GiB (> L2), so no L2 flush is needed.  `value` is device throughput
-(Mkeys/s, CUDA events over the K steps); `e2e` is the same metric through the
-C ABI with the keys/values starting and ending in pinned host memory.
+(mgpu_radix_sort).  Before each step a device copy restores an unsorted input
+(outside the step's CUDA event pair); the input is 2 GiB (> L2), so no L2
+flush is needed.  `value` is device throughput (Mkeys/s from the mean of the
+per-step event times); `e2e` is the same metric through the C ABI with the
+keys/values starting and ending in pinned host memory.
 `roofline` covers the dominant kernel (onesweep_pass): 16 algorithmic bytes
 per key per launch, divided by its mean event-timed duration.
 
@@ -46,7 +46,8 @@ def config(dist="uniform"):
         "key_dtype": "u32",
         "val_dtype": "u32",
         "digit_bits": 8,
-        "l2": "inputs larger than L2 (2 GiB per step, one unsorted copy per step)",
+        "l2": "inputs larger than L2 (2 GiB unsorted input restored before each step, "
+              "outside the step's events)",
         "seed": SEED,
     }
 
@@ -81,7 +82,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
-                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -132,7 +133,7 @@ def cpu_baseline(threads, sample=CPU_SAMPLE, min_seconds=10.0, max_reps=8):
         k = k0.copy()
         v = v0.copy()
         t = time.perf_counter()
-        oracle.sort_parallel_inplace(k, v, 2, threads)
+        oracle.sort_parallel_inplace(k, v, "radix", threads)
         dt = time.perf_counter() - t
         t_total += dt
         rates.append(sample / dt / 1e6)
@@ -148,12 +149,12 @@ def run_reference(args):
     k0, v0 = make_input(CPU_SAMPLE)
     for _ in range(args.warmup):
         k, v = k0.copy(), v0.copy()
-        oracle.sort_parallel_inplace(k, v, 2, threads)
+        oracle.sort_parallel_inplace(k, v, "radix", threads)
     times = []
     for _ in range(args.steps):
         k, v = k0.copy(), v0.copy()
         t = time.perf_counter()
-        oracle.sort_parallel_inplace(k, v, 2, threads)
+        oracle.sort_parallel_inplace(k, v, "radix", threads)
         times.append(time.perf_counter() - t)
     value = CPU_SAMPLE * len(times) / sum(times) / 1e6
     sample = "%d-key sample of the workload per step (same generator and seed)" % CPU_SAMPLE
@@ -177,7 +178,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mgpu", choices=["mgpu", "reference"])
     ap.add_argument("--n", type=int, default=N_KEYS)
@@ -202,67 +203,69 @@ def main():
     ctx = mg.Context(local)
     keys_h, vals_h = make_input(n, seed=SEED + rank)
 
-    # One unsorted device copy per timed step (each > L2).
+    # Each step sorts an unsorted 2 GiB copy (> L2), restored from the pristine
+    # input by a device copy that lies outside the step's event pair.
     pristine_k = mg.DeviceArray.from_numpy(keys_h)
     pristine_v = mg.DeviceArray.from_numpy(vals_h)
-    copies = [(mg.DeviceArray(n, np.uint32), mg.DeviceArray(n, np.uint32)) for _ in range(steps)]
+    copies = [(mg.DeviceArray(n, np.uint32), mg.DeviceArray(n, np.uint32)) for _ in range(2)]
 
     def restore(i):
-        copies[i][0].copy_from(pristine_k)
-        copies[i][1].copy_from(pristine_v)
+        copies[i % 2][0].copy_from(pristine_k)
+        copies[i % 2][1].copy_from(pristine_v)
 
     aux_bytes = ctx.radix_sort_aux_size(np.uint32, np.uint32, n)
     aux_t = torch.empty(aux_bytes, dtype=torch.uint8, device="cuda")
     aux = (aux_t.data_ptr(), aux_bytes)
 
     for w in range(warmup):
-        restore(0)
-        ctx.radix_sort(copies[0][0], copies[0][1], aux=aux)
-    for i in range(steps):
-        restore(i)
+        restore(w)
+        ctx.radix_sort(copies[w % 2][0], copies[w % 2][1], aux=aux)
     ctx.synchronize()
     torch.cuda.synchronize()
 
     stream = torch.cuda.current_stream()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
-    launches0 = ctx.launch_count
-    start.record(stream)
+    launches = 0
     for i in range(steps):
-        ctx.radix_sort(copies[i][0], copies[i][1], aux=aux)
-    end.record(stream)
+        restore(i)
+        ev[i][0].record(stream)
+        l0 = ctx.launch_count
+        ctx.radix_sort(copies[i % 2][0], copies[i % 2][1], aux=aux)
+        launches += ctx.launch_count - l0
+        ev[i][1].record(stream)
     torch.cuda.synchronize()
-    launches = ctx.launch_count - launches0
     if pg:
         pg.barrier()
     clk = clocks.stop()
     ctx.synchronize()
-    ms = start.elapsed_time(end) / steps
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(step_ms) / steps
     if pg:
         t = torch.tensor([ms], device="cuda")
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         ms = float(t.item())
 
-    # Correctness of the timed output (cheap properties on one copy).
-    gk = copies[0][0].numpy()
-    gv = copies[0][1].numpy()
+    # Correctness of the last timed output (cheap properties).
+    gk = copies[(steps - 1) % 2][0].numpy()
+    gv = copies[(steps - 1) % 2][1].numpy()
     ok_sorted = bool(np.all(gk[1:] >= gk[:-1])) and bool(np.array_equal(keys_h[gv], gk))
 
     # Per-kernel event timing for the roofline (same workload, fresh copies).
-    prof_steps = min(steps, 3)
+    prof_steps = min(steps, 4)
+    ctx.synchronize()
     for i in range(prof_steps):
         restore(i)
-    ctx.synchronize()
-    ctx.profile(True)
-    for i in range(prof_steps):
-        ctx.radix_sort(copies[i][0], copies[i][1], aux=aux)
+        ctx.profile(True)
+        ctx.radix_sort(copies[i % 2][0], copies[i % 2][1], aux=aux)
+        ctx.profile(False)
     prof = ctx.profile_read()
-    ctx.profile(False)
     p_launches, p_ms = prof.get("onesweep_pass", (0, 0.0))
     pass_ms = p_ms / max(1, p_launches)
     achieved = PASS_BYTES_PER_KEY * n / (pass_ms * 1e-3) / 1e9 if pass_ms else None

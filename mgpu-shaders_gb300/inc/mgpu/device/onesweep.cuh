@@ -133,37 +133,61 @@ radix_histogram(const K* keys, int64_t count, uint32_t* hist, uint4* zero, int64
     if(sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS>
-__global__ void __launch_bounds__(NT, MIN_BLOCKS)
-onesweep_pass(onesweep_args<K, V> a) {
+// Where one tile of a sort sits.  A plain sort is one sequence; a segmented
+// sort runs one independent sort per large segment over the same kernel.
+struct onesweep_tile_t {
+  int64_t base;            // first element of the tile (absolute index)
+  int valid;               // elements in the tile
+  int local;               // tile index within its sort (tile 0 publishes inclusive)
+  uint32_t* lb_row;        // this tile's look-back row; predecessor k is lb_row - 256 k
+  const uint32_t* hist;    // this pass's 256 digit totals of the tile's sort
+  int64_t out_base;        // absolute index of the sort's first element
+};
+
+// Claims the next tile id and prepares shared memory (barrier, counters).
+// Returns the tile id; every thread of the CTA must call it.
+template<typename K, typename V, int NT, int ITEMS>
+__device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned char* smem) {
+  typedef onesweep_layout<K, V, NT, ITEMS> L;
+  uint32_t* whist = (uint32_t*)(smem + L::hist_off);
+  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
+  int* s_tile = (int*)(smem + L::tile_off);
+  const int tid = threadIdx.x;
+  if(tid == 0) {
+    *s_tile = (int)atomicAdd(tile_counter, 1u);
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
+  __syncthreads();
+  return *s_tile;
+}
+
+template<typename K, typename V, int NT, int ITEMS>
+__device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
+  const onesweep_tile_t& t, unsigned char* smem) {
   typedef onesweep_layout<K, V, NT, ITEMS> L;
   typedef typename L::U U;
   constexpr int TILE = L::tile;
   constexpr int NWARPS = L::num_warps;
   constexpr bool HAS_V = L::has_values;
 
-  extern __shared__ __align__(16) unsigned char smem[];
   U* ks = (U*)(smem + L::keys_off);
   V* vs = (V*)(smem + L::vals_off);
   uint32_t* whist = (uint32_t*)(smem + L::hist_off);
   int* gbase = (int*)(smem + L::gbase_off);
   uint32_t* stmp = (uint32_t*)(smem + L::scan_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
-  int* s_tile = (int*)(smem + L::tile_off);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if(tid == 0) {
-    *s_tile = (int)atomicAdd(a.tile_counter, 1u);
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  for(int i = tid; i < NWARPS * radix_bins; i += NT) whist[i] = 0;
-  __syncthreads();
-
-  const int tile = *s_tile;
-  const int64_t base = (int64_t)tile * TILE;
-  const int valid = (int)min((int64_t)TILE, a.count - base);
-  const bool bulk = a.tma && valid == TILE;
+  const int64_t base = t.base;
+  const int valid = t.valid;
+  const int tile = t.local;
+  // a.tma: both arrays start on 16 bytes; a tile qualifies when it is full
+  // and starts on a whole vector of keys and of values.
+  constexpr int64_t vec_mask = (16 / sizeof(U) > (HAS_V ? 16 / sizeof(V) : 1) ?
+    16 / sizeof(U) : (HAS_V ? 16 / sizeof(V) : 1)) - 1;
+  const bool bulk = a.tma && valid == TILE && 0 == (base & vec_mask);
 
   if(bulk && tid == 0) {
     constexpr uint32_t kbytes = sizeof(U) * TILE;
@@ -235,9 +259,8 @@ onesweep_pass(onesweep_args<K, V> a) {
       tile_cnt += c;
     }
     valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
-    st_relaxed(&a.lookback[(int64_t)tile * radix_bins + tid],
-      (tile ? lb_agg : lb_inc) | valid_cnt);
-    glob_cnt = a.hist[tid];
+    st_relaxed(&t.lb_row[tid], (tile ? lb_agg : lb_inc) | valid_cnt);
+    glob_cnt = t.hist[tid];
   }
   uint32_t tile_start = tile_cnt, glob_start = glob_cnt;
   scan_256_pair(tile_start, glob_start, stmp);
@@ -245,10 +268,10 @@ onesweep_pass(onesweep_args<K, V> a) {
   if(tid < radix_bins) {
     uint32_t excl = 0;
     if(tile > 0) {
-      int j = tile - 1;
+      const uint32_t* pred = t.lb_row + tid - radix_bins;
       int spins = 0;
       while(true) {
-        uint32_t s = ld_relaxed(&a.lookback[(int64_t)j * radix_bins + tid]);
+        uint32_t s = ld_relaxed(pred);
         uint32_t flag = s & ~lb_count;
         if(!flag) {
           ++spins;
@@ -261,9 +284,9 @@ onesweep_pass(onesweep_args<K, V> a) {
         }
         excl += s & lb_count;
         if(flag == lb_inc) break;
-        --j;
+        pred -= radix_bins;
       }
-      st_relaxed(&a.lookback[(int64_t)tile * radix_bins + tid], lb_inc | (excl + valid_cnt));
+      st_relaxed(&t.lb_row[tid], lb_inc | (excl + valid_cnt));
     }
     gbase[tid] = (int)(glob_start + excl - tile_start);
 #pragma unroll 4
@@ -298,6 +321,8 @@ onesweep_pass(onesweep_args<K, V> a) {
   // Write out in local order: consecutive threads hit consecutive addresses
   // inside each digit's run.
   const int out_rem = valid - tid;
+  U* keys_out = a.keys_out + t.out_base;
+  V* vals_out = a.vals_out + t.out_base;
 #pragma unroll
   for(int j = 0; j < ITEMS; ++j) {
     int idx = j * NT + tid;
@@ -307,13 +332,29 @@ onesweep_pass(onesweep_args<K, V> a) {
       uint32_t dst = (uint32_t)gbase[d] + idx;
       if(a.last) {
         K key = radix_key<K>::from_bits(u);
-        memcpy(&a.keys_out[dst], &key, sizeof(K));
+        memcpy(&keys_out[dst], &key, sizeof(K));
       } else {
-        a.keys_out[dst] = u;
+        keys_out[dst] = u;
       }
-      if constexpr(HAS_V) a.vals_out[dst] = vs[idx];
+      if constexpr(HAS_V) vals_out[dst] = vs[idx];
     }
   }
+}
+
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS>
+__global__ void __launch_bounds__(NT, MIN_BLOCKS)
+onesweep_pass(onesweep_args<K, V> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int TILE = NT * ITEMS;
+  const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
+  onesweep_tile_t t;
+  t.base = (int64_t)tile * TILE;
+  t.valid = (int)min((int64_t)TILE, a.count - t.base);
+  t.local = tile;
+  t.lb_row = a.lookback + (int64_t)tile * radix_bins;
+  t.hist = a.hist;
+  t.out_base = 0;
+  onesweep_tile<K, V, NT, ITEMS>(a, t, smem);
 }
 
 }  // namespace device

@@ -58,8 +58,10 @@ template<typename T> struct min_t {
 enum : uint32_t { status_invalid = 0, status_aggregate = 1, status_inclusive = 2 };
 
 // Per-tile look-back status.  4-byte values share one 64-bit word with their
-// flag (a single store publishes both); 8-byte values use a value word and a
-// flag word ordered by release/acquire.
+// flag (a single store publishes both).  8-byte values use one value word per
+// status (aggregate, inclusive) and a flag word ordered by release/acquire; a
+// reader loads the value slot of the flag it saw, so a later inclusive
+// publication can never be mistaken for the aggregate.
 template<typename T, bool wide = (sizeof(T) == 8)>
 struct tile_status_t;
 
@@ -83,23 +85,25 @@ struct tile_status_t<T, false> {
 
 template<typename T>
 struct tile_status_t<T, true> {
-  uint64_t* values;
+  uint64_t* values;          // [2][tiles]: aggregate slot, inclusive slot
   uint32_t* flags;
-  static size_t bytes(int64_t tiles) { return (sizeof(uint64_t) + sizeof(uint32_t)) * tiles + 16; }
-  __host__ __device__ void bind(void* p, int64_t tiles) {
+  int64_t tiles;
+  static size_t bytes(int64_t tiles) { return (2 * sizeof(uint64_t) + sizeof(uint32_t)) * tiles + 16; }
+  __host__ __device__ void bind(void* p, int64_t n) {
     values = (uint64_t*)p;
-    flags = (uint32_t*)(values + tiles);
+    flags = (uint32_t*)(values + 2 * n);
+    tiles = n;
   }
   __device__ __forceinline__ void publish(int64_t tile, uint32_t flag, T v) const {
     uint64_t b;
     memcpy(&b, &v, 8);
-    st_relaxed(values + tile, b);
+    st_relaxed(values + (flag == status_inclusive ? tiles : 0) + tile, b);
     st_release(flags + tile, flag);
   }
   __device__ __forceinline__ uint32_t read(int64_t tile, T& v) const {
     uint32_t f = ld_acquire(flags + tile);
     if(f) {
-      uint64_t b = ld_relaxed(values + tile);
+      uint64_t b = ld_relaxed(values + (f == status_inclusive ? tiles : 0) + tile);
       memcpy(&v, &b, 8);
     }
     return f;

@@ -1,0 +1,558 @@
+// Batched segmented sort and segmented scan for sm_103a.
+//
+// No reference counterpart: the reference sorts one array per call
+// (vk/radix.hxx:195-470), so many small arrays cost a launch sequence each.
+// Here all segments of a CSR layout (offsets[s] .. offsets[s+1]) are sorted
+// by one fixed launch sequence, whatever their number:
+//
+//  1. seg_classify: one pass over the offsets puts each segment in a size
+//     class: <= 32 keys (one warp, rank sort in registers), <= 32*items keys
+//     (one warp, LSD radix in a shared-memory slice), <= one tile (one CTA,
+//     LSD radix in shared memory), larger (multi-CTA onesweep).  Large
+//     segments get contiguous tile ranges and zeroed histogram rows.
+//  2. seg_small_sort: one persistent launch; CTAs pull CTA-class segments,
+//     then warps pull warp-class segments, from atomic queues.
+//  3. seg_histogram + per-digit onesweep passes over all large segments'
+//     tiles together; each tile looks back only within its own segment.
+//
+// Sort order within a segment is the radix_sort order (radix_permute_t bits),
+// stable; values follow their keys.
+#pragma once
+
+#include "common.cuh"
+#include "onesweep.cuh"
+#include "scan.cuh"
+
+namespace mgpu {
+namespace device {
+
+// Counters and work lists of one segmented sort (device memory).
+struct seg_state_t {
+  uint32_t* counters;        // see seg_counter_t
+  int* warp_list;            // segments of 2..32 keys
+  int* slice_list;           // segments of 33..slice keys
+  int* cta_list;             // segments of slice+1..tile keys
+  int* large_seg;            // segments above one tile
+  int* large_tile_base;      // first global tile of each large segment
+  int* tile_owner;           // large-segment index of each global tile
+  uint32_t* seg_hist;        // [large][passes][256] digit totals
+  uint32_t* lookback;        // [passes][max_tiles][256] look-back words
+  int64_t max_tiles;         // bound on the large segments' tiles
+};
+
+enum seg_counter_t {
+  sc_warp = 0, sc_slice, sc_cta, sc_large, sc_tiles,
+  sc_next_cta, sc_next_warp, sc_next_slice, sc_pass_tiles /* + pass */, sc_count = sc_pass_tiles + 8
+};
+
+template<int TILE, int SLICE, int PASSES>
+__global__ void seg_classify(const int64_t* offsets, int64_t num_segments, seg_state_t s) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_segments; i += stride) {
+    int64_t b = offsets[i], e = offsets[i + 1];
+    int64_t n = e - b;
+    if(n <= 1) continue;
+    if(n <= 32) {
+      s.warp_list[atomicAdd(&s.counters[sc_warp], 1u)] = (int)i;
+    } else if(n <= SLICE) {
+      s.slice_list[atomicAdd(&s.counters[sc_slice], 1u)] = (int)i;
+    } else if(n <= TILE) {
+      s.cta_list[atomicAdd(&s.counters[sc_cta], 1u)] = (int)i;
+    } else {
+      int tiles = (int)div_up(n, TILE);
+      int l = (int)atomicAdd(&s.counters[sc_large], 1u);
+      int tb = (int)atomicAdd(&s.counters[sc_tiles], (uint32_t)tiles);
+      s.large_seg[l] = (int)i;
+      s.large_tile_base[l] = tb;
+      for(int t = 0; t < tiles; ++t) s.tile_owner[tb + t] = l;
+      uint4* h = (uint4*)(s.seg_hist + (int64_t)l * PASSES * radix_bins);
+      for(int j = 0; j < PASSES * radix_bins / 4; ++j) h[j] = make_uint4(0, 0, 0, 0);
+    }
+  }
+}
+
+// Stable rank sort of one segment of at most 32 keys by one warp: each lane
+// holds one key; rank = keys below + equal keys in lower lanes.
+template<typename K, typename V>
+__device__ __forceinline__ void warp_rank_sort(K* keys, V* vals, int n) {
+  typedef typename radix_key<K>::bits_t U;
+  constexpr bool HAS_V = !std::is_same<V, no_values>::value;
+  const int lane = threadIdx.x & 31;
+  U u = ~(U)0;
+  K key{};
+  V val{};
+  if(lane < n) {
+    key = keys[lane];
+    u = radix_key<K>::to_bits(key);
+    if constexpr(HAS_V) val = vals[lane];
+  }
+  int rank = 0;
+#pragma unroll
+  for(int j = 0; j < 32; ++j) {
+    U o = __shfl_sync(0xffffffffu, u, j);
+    rank += (o < u) || (o == u && j < lane);
+  }
+  __syncwarp();
+  if(lane < n) {
+    keys[rank] = key;
+    if constexpr(HAS_V) vals[rank] = val;
+  }
+}
+
+// Stable LSD radix sort (8-bit digits) of n <= 32 * W * ITEMS keys held in a
+// shared-memory slice, by a group of W warps.  gtid is the thread's index in
+// the group; hist has W * 256 words; tmp has W words.  Keys are radix bits.
+template<int W, int ITEMS, typename U, typename V>
+__device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* hist,
+  uint32_t* tmp, int passes, int gtid) {
+  constexpr bool HAS_V = !std::is_same<V, no_values>::value;
+  constexpr int G = 32 * W;
+  constexpr int DPT = radix_bins / G;          // digits per thread
+  static_assert(radix_bins % G == 0, "group size divides 256");
+  const int lane = gtid & 31, gw = gtid >> 5;
+  const int warp_base = gw * 32 * ITEMS;
+  const int rem = n - warp_base - lane;
+  const uint32_t lt_mask = lanemask_lt();
+  auto gsync = [] { if(W == 1) __syncwarp(); else __syncthreads(); };
+  for(int pass = 0; pass < passes; ++pass) {
+    const int shift = 8 * pass;
+    for(int i = gtid; i < W * radix_bins; i += G) hist[i] = 0;
+    U k[ITEMS];
+    V v[ITEMS];
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      bool in = 32 * i < rem;
+      k[i] = in ? ks[warp_base + 32 * i + lane] : ~(U)0;
+      if constexpr(HAS_V) v[i] = in ? vs[warp_base + 32 * i + lane] : V();
+    }
+    gsync();
+    uint32_t r[ITEMS];
+    uint32_t* wh = hist + gw * radix_bins;
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      uint32_t d = extract_digit(k[i], shift, 8);
+      uint32_t peers = __match_any_sync(0xffffffffu, d);
+      uint32_t below = peers & lt_mask;
+      uint32_t cnt = wh[d];
+      __syncwarp();
+      if(!below) wh[d] = cnt + __popc(peers);
+      __syncwarp();
+      r[i] = cnt + __popc(below);
+    }
+    gsync();
+    uint32_t tot[DPT];
+    uint32_t sum = 0;
+#pragma unroll
+    for(int j = 0; j < DPT; ++j) {
+      int d = gtid * DPT + j;
+      uint32_t t = 0;
+      for(int w = 0; w < W; ++w) {
+        uint32_t c = hist[w * radix_bins + d];
+        hist[w * radix_bins + d] = t;
+        t += c;
+      }
+      tot[j] = t;
+      sum += t;
+    }
+    // Exclusive scan of `sum` over the group's threads.
+    uint32_t inc = sum;
+#pragma unroll
+    for(int off = 1; off < 32; off <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+      if(lane >= off) inc += y;
+    }
+    uint32_t excl = inc - sum;
+    if(W > 1) {
+      if(lane == 31) tmp[gw] = inc;
+      gsync();
+      for(int w = 0; w < gw; ++w) excl += tmp[w];
+    }
+#pragma unroll
+    for(int j = 0; j < DPT; ++j) {
+      int d = gtid * DPT + j;
+      for(int w = 0; w < W; ++w) hist[w * radix_bins + d] += excl;
+      excl += tot[j];
+    }
+    gsync();
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      uint32_t d = extract_digit(k[i], shift, 8);
+      uint32_t pos = r[i] + wh[d];
+      ks[pos] = k[i];
+      if constexpr(HAS_V) vs[pos] = v[i];
+    }
+    gsync();
+  }
+}
+
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS>
+struct seg_small_layout {
+  typedef typename radix_key<K>::bits_t U;
+  static constexpr bool has_values = !std::is_same<V, no_values>::value;
+  static constexpr int tile = NT * ITEMS;
+  static constexpr int slice = 32 * SLICE_ITEMS;
+  static constexpr int warps = NT / 32;
+  static constexpr size_t keys_off = 0;
+  static constexpr size_t vals_off = sizeof(U) * tile;
+  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
+  static constexpr size_t tmp_off = hist_off + sizeof(uint32_t) * warps * radix_bins;
+  static constexpr size_t misc_off = tmp_off + sizeof(uint32_t) * 32;
+  static constexpr size_t bytes = misc_off + 16;
+  static_assert(warps * slice <= tile, "warp slices fit in the tile buffers");
+};
+
+// Persistent sort of every segment up to one tile: CTA-class segments first
+// (whole CTA), then slice-class and warp-class segments (one warp each).
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES>
+__global__ void __launch_bounds__(NT)
+seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
+  typedef typename L::U U;
+  constexpr bool HAS_V = L::has_values;
+  extern __shared__ __align__(16) unsigned char smem[];
+  U* ks = (U*)(smem + L::keys_off);
+  V* vs = (V*)(smem + L::vals_off);
+  uint32_t* hist = (uint32_t*)(smem + L::hist_off);
+  uint32_t* tmp = (uint32_t*)(smem + L::tmp_off);
+  int* s_item = (int*)(smem + L::misc_off);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // CTA-class segments.
+  const uint32_t num_cta = s.counters[sc_cta];
+  while(true) {
+    if(tid == 0) *s_item = (int)atomicAdd(&s.counters[sc_next_cta], 1u);
+    __syncthreads();
+    const int item = *s_item;
+    __syncthreads();
+    if((uint32_t)item >= num_cta) break;
+    const int seg = s.cta_list[item];
+    const int64_t b = offsets[seg];
+    const int n = (int)(offsets[seg + 1] - b);
+    for(int i = tid; i < n; i += NT) {
+      ks[i] = radix_key<K>::to_bits(keys[b + i]);
+      if constexpr(HAS_V) vs[i] = vals[b + i];
+    }
+    __syncthreads();
+    group_radix_sort<NT / 32, ITEMS>(ks, vs, n, hist, tmp, PASSES, tid);
+    for(int i = tid; i < n; i += NT) {
+      keys[b + i] = radix_key<K>::from_bits(ks[i]);
+      if constexpr(HAS_V) vals[b + i] = vs[i];
+    }
+    __syncthreads();
+  }
+
+  // Slice-class segments: each warp sorts its own in a private slice.
+  const uint32_t num_slice = s.counters[sc_slice];
+  U* wks = ks + warp * L::slice;
+  V* wvs = vs + warp * L::slice;
+  uint32_t* wh = hist + warp * radix_bins;
+  while(true) {
+    int item = 0;
+    if(lane == 0) item = (int)atomicAdd(&s.counters[sc_next_slice], 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if((uint32_t)item >= num_slice) break;
+    const int seg = s.slice_list[item];
+    const int64_t b = offsets[seg];
+    const int n = (int)(offsets[seg + 1] - b);
+    for(int i = lane; i < n; i += 32) {
+      wks[i] = radix_key<K>::to_bits(keys[b + i]);
+      if constexpr(HAS_V) wvs[i] = vals[b + i];
+    }
+    __syncwarp();
+    group_radix_sort<1, SLICE_ITEMS>(wks, wvs, n, wh, nullptr, PASSES, lane);
+    for(int i = lane; i < n; i += 32) {
+      keys[b + i] = radix_key<K>::from_bits(wks[i]);
+      if constexpr(HAS_V) vals[b + i] = wvs[i];
+    }
+    __syncwarp();
+  }
+
+  // Warp-class segments: rank sort in registers.
+  const uint32_t num_warp = s.counters[sc_warp];
+  while(true) {
+    int item = 0;
+    if(lane == 0) item = (int)atomicAdd(&s.counters[sc_next_warp], 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if((uint32_t)item >= num_warp) break;
+    const int seg = s.warp_list[item];
+    const int64_t b = offsets[seg];
+    const int n = (int)(offsets[seg + 1] - b);
+    warp_rank_sort<K, V>(keys + b, HAS_V ? vals + b : vals, n);
+  }
+}
+
+// Digit totals of every large segment, all passes, one read of the keys.
+// Each CTA walks a contiguous range of global tiles and flushes its shared
+// histogram whenever the owning segment changes.  Also clears the look-back
+// words of all used tiles.
+template<typename K, int NT, int TILE, int PASSES>
+__global__ void __launch_bounds__(NT)
+seg_histogram(const K* keys, const int64_t* offsets, seg_state_t s) {
+  typedef typename radix_key<K>::bits_t U;
+  __shared__ uint32_t sh[PASSES * radix_bins];
+  const int tid = threadIdx.x;
+  const int num_tiles = (int)s.counters[sc_tiles];
+  const int per = (int)div_up(num_tiles, gridDim.x);
+  const int t0 = blockIdx.x * per, t1 = min(num_tiles, t0 + per);
+  // Clear this CTA's tiles' look-back rows (all passes).
+  for(int p = 0; p < PASSES; ++p) {
+    uint4* z = (uint4*)(s.lookback + ((int64_t)p * s.max_tiles + t0) * radix_bins);
+    int64_t words = (int64_t)max(0, t1 - t0) * radix_bins / 4;
+    for(int64_t i = tid; i < words; i += NT) z[i] = make_uint4(0, 0, 0, 0);
+  }
+  int cur = -1;
+  auto flush = [&] {
+    __syncthreads();
+    if(cur >= 0) {
+      uint32_t* g = s.seg_hist + (int64_t)cur * PASSES * radix_bins;
+      for(int i = tid; i < PASSES * radix_bins; i += NT) {
+        if(sh[i]) atomicAdd(&g[i], sh[i]);
+        sh[i] = 0;
+      }
+    } else {
+      for(int i = tid; i < PASSES * radix_bins; i += NT) sh[i] = 0;
+    }
+    __syncthreads();
+  };
+  flush();
+  for(int t = t0; t < t1; ++t) {
+    const int l = s.tile_owner[t];
+    if(l != cur) { flush(); cur = l; }
+    const int seg = s.large_seg[l];
+    const int64_t sb = offsets[seg], se = offsets[seg + 1];
+    const int64_t b = sb + (int64_t)(t - s.large_tile_base[l]) * TILE;
+    const int n = (int)min((int64_t)TILE, se - b);
+    for(int i = tid; i < n; i += NT) {
+      U u = radix_key<K>::to_bits(keys[b + i]);
+#pragma unroll
+      for(int p = 0; p < PASSES; ++p)
+        atomicAdd(&sh[p * radix_bins + extract_digit(u, 8 * p, 8)], 1u);
+    }
+  }
+  flush();
+}
+
+// One digit pass over the tiles of all large segments.
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int PASSES>
+__global__ void __launch_bounds__(NT, MIN_BLOCKS)
+seg_onesweep_pass(onesweep_args<K, V> a, const int64_t* offsets, seg_state_t s, int pass) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int TILE = NT * ITEMS;
+  if(blockIdx.x >= s.counters[sc_tiles]) return;
+  const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
+  const int l = s.tile_owner[tile];
+  const int seg = s.large_seg[l];
+  const int64_t sb = offsets[seg], se = offsets[seg + 1];
+  const int local = tile - s.large_tile_base[l];
+  onesweep_tile_t t;
+  t.base = sb + (int64_t)local * TILE;
+  t.valid = (int)min((int64_t)TILE, se - t.base);
+  t.local = local;
+  t.lb_row = s.lookback + ((int64_t)pass * s.max_tiles + tile) * radix_bins;
+  t.hist = s.seg_hist + ((int64_t)l * PASSES + pass) * radix_bins;
+  t.out_base = sb;
+  onesweep_tile<K, V, NT, ITEMS>(a, t, smem);
+}
+
+////////////////////////////////////////////////////////////////////////////////
+// Segmented scan: a single-pass look-back scan over (head flag, value) pairs
+// with the operator (fa, a) . (fb, b) = (fa | fb, fb ? b : a op b), which is
+// associative, so one chained scan restarts at every segment head.  A tile's
+// look-back also stops early at any predecessor whose aggregate contains a
+// head, since nothing before it reaches this tile.
+
+// First segment whose begin offset is >= each tile's first element.
+__global__ inline void seg_tile_first(const int64_t* offsets, int64_t num_segments, int64_t tile,
+  int64_t num_tiles, int* first) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(t >= num_tiles) return;
+  int64_t pos = t * tile;
+  int64_t lo = 0, hi = num_segments;   // lower_bound over offsets[0, num_segments)
+  while(lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if(offsets[mid] < pos) lo = mid + 1;
+    else hi = mid;
+  }
+  first[t] = (int)lo;
+}
+
+template<typename T>
+struct seg_pair_t {
+  T v;
+  uint32_t f;
+};
+
+template<typename T, typename op_t>
+__device__ __forceinline__ seg_pair_t<T> seg_combine(seg_pair_t<T> a, seg_pair_t<T> b, op_t op) {
+  return { b.f ? b.v : op(a.v, b.v), a.f | b.f };
+}
+
+// Status of a tile: flag word (status | head << 2) and one value word per
+// status ([2][tiles]: aggregate slot, inclusive slot), so a reader always
+// loads the value that belongs to the flag it observed.
+template<typename T>
+struct seg_status_t {
+  uint32_t* flags;
+  uint64_t* values;
+  int64_t tiles;
+  __device__ __forceinline__ void publish(int64_t tile, uint32_t status, seg_pair_t<T> p) const {
+    uint64_t b = 0;
+    memcpy(&b, &p.v, sizeof(T));
+    st_relaxed(values + (status == status_inclusive ? tiles : 0) + tile, b);
+    st_release(flags + tile, status | (p.f << 2));
+  }
+  __device__ __forceinline__ uint32_t read(int64_t tile, seg_pair_t<T>& p) const {
+    uint32_t w = ld_acquire(flags + tile);
+    if(w & 3) {
+      uint64_t b = ld_relaxed(values + ((w & 3) == status_inclusive ? tiles : 0) + tile);
+      memcpy(&p.v, &b, sizeof(T));
+      p.f = (w >> 2) & 1;
+    }
+    return w & 3;
+  }
+};
+
+template<typename T, typename op_t, int NT, int VT, bool exclusive>
+__global__ void __launch_bounds__(NT)
+seg_scan_kernel(const T* in, T* out, int64_t count, const int64_t* offsets, int64_t num_segments,
+  const int* tile_first, T init, op_t op, seg_status_t<T> st, uint32_t* tile_counter,
+  int* error) {
+  typedef seg_pair_t<T> P;
+  constexpr int TILE = NT * VT;
+  constexpr int NW = NT / 32;
+  __shared__ uint32_t heads[TILE / 32];
+  __shared__ T wv[NW];
+  __shared__ uint32_t wf[NW];
+  __shared__ T s_pv;
+  __shared__ uint32_t s_pf;
+  __shared__ int64_t s_tile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if(tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+  for(int i = tid; i < TILE / 32; i += NT) heads[i] = 0;
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t base = tile * TILE;
+  const int valid = (int)min((int64_t)TILE, count - base);
+
+  // Mark the heads of the non-empty segments that start in this tile.
+  for(int64_t s = tile_first[tile] + tid; s < num_segments; s += NT) {
+    int64_t o = offsets[s];
+    if(o >= base + valid) break;
+    if(offsets[s + 1] > o && o >= base) {
+      int r = (int)(o - base);
+      atomicOr(&heads[r >> 5], 1u << (r & 31));
+    }
+  }
+  if(tile == 0 && tid == 0) atomicOr(&heads[0], 1u);
+  __syncthreads();
+
+  const int first = tid * VT;
+  T x[VT];
+  load_thread<T, VT>(in + base + first, valid - first, false, x, op_t::identity());
+  uint32_t hbits = 0;
+#pragma unroll
+  for(int i = 0; i < VT; ++i) {
+    int e = first + i;
+    hbits |= ((heads[e >> 5] >> (e & 31)) & 1u) << i;
+  }
+  // Inclusive pair scan inside the thread.
+  P acc { x[0], hbits & 1u };
+  T incv[VT];
+  incv[0] = x[0];
+#pragma unroll
+  for(int i = 1; i < VT; ++i) {
+    acc = seg_combine<T>(acc, P { x[i], (hbits >> i) & 1u }, op);
+    incv[i] = acc.v;
+  }
+  // Warp-inclusive scan of thread aggregates.
+  P w = acc;
+#pragma unroll
+  for(int off = 1; off < 32; off <<= 1) {
+    P y { __shfl_up_sync(0xffffffffu, w.v, off), __shfl_up_sync(0xffffffffu, w.f, off) };
+    if(lane >= off) w = seg_combine<T>(y, w, op);
+  }
+  P wex { __shfl_up_sync(0xffffffffu, w.v, 1), __shfl_up_sync(0xffffffffu, w.f, 1) };
+  if(lane == 31) { wv[warp] = w.v; wf[warp] = w.f; }
+  __syncthreads();
+  if(warp == 0) {
+    P t { op_t::identity(), 0u };
+    if(lane < NW) t = P { wv[lane], wf[lane] };
+#pragma unroll
+    for(int off = 1; off < 32; off <<= 1) {
+      P y { __shfl_up_sync(0xffffffffu, t.v, off), __shfl_up_sync(0xffffffffu, t.f, off) };
+      if(lane >= off) t = seg_combine<T>(y, t, op);
+    }
+    if(lane < NW) { wv[lane] = t.v; wf[lane] = t.f; }
+  }
+  __syncthreads();
+  const P tile_agg { wv[NW - 1], wf[NW - 1] };
+  // Exclusive prefix of this thread within the tile (identity pair when none).
+  P tex { op_t::identity(), 0u };
+  if(lane) tex = wex;
+  if(warp) tex = seg_combine<T>(P { wv[warp - 1], wf[warp - 1] }, tex, op);
+
+  if(warp == 0) {
+    P prefix { op_t::identity(), 0u };
+    if(tile == 0) {
+      if(lane == 0) st.publish(0, status_inclusive, tile_agg);
+    } else {
+      if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
+      bool have = false;
+      int64_t b0 = tile - 1;
+      while(true) {
+        int64_t j = b0 - lane;
+        P v { op_t::identity(), 0u };
+        uint32_t flag = status_inclusive;
+        if(j >= 0) {
+          int spins = 0;
+          while(true) {
+            flag = st.read(j, v);
+            if(flag != status_invalid) break;
+            if(++spins >= spin_limit ||
+               (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
+              raise_error(error, err_lookback_timeout);
+              flag = status_inclusive;
+              v = P { op_t::identity(), 0u };
+              break;
+            }
+          }
+        }
+        // Stop at an inclusive prefix or at any tile containing a head.
+        uint32_t stop = __ballot_sync(0xffffffffu, flag == status_inclusive || v.f);
+        int limit = stop ? __ffs(stop) - 1 : 31;
+#pragma unroll
+        for(int off = 1; off < 32; off <<= 1) {
+          P y { __shfl_down_sync(0xffffffffu, v.v, off), __shfl_down_sync(0xffffffffu, v.f, off) };
+          if(lane + off <= limit) v = seg_combine<T>(y, v, op);
+        }
+        P r { __shfl_sync(0xffffffffu, v.v, 0), __shfl_sync(0xffffffffu, v.f, 0) };
+        prefix = have ? seg_combine<T>(r, prefix, op) : r;
+        have = true;
+        if(stop) break;
+        b0 -= 32;
+      }
+      if(lane == 0) st.publish(tile, status_inclusive, seg_combine<T>(prefix, tile_agg, op));
+    }
+    if(lane == 0) { s_pv = prefix.v; s_pf = prefix.f; }
+  }
+  __syncthreads();
+  // Carry into the thread = prefix . tex; element i's inclusive pair is
+  // carry . (local pairs 0..i).  A head inside the thread cuts the carry.
+  const P carry = seg_combine<T>(P { s_pv, s_pf }, tex, op);
+  T y[VT];
+  bool seen_head = false;
+#pragma unroll
+  for(int i = 0; i < VT; ++i) {
+    bool h = (hbits >> i) & 1u;
+    // Exclusive value before element i within its segment.
+    T before = (i == 0) ? carry.v : (seen_head ? incv[i - 1] : op(carry.v, incv[i - 1]));
+    seen_head |= h;
+    T incl = seen_head ? incv[i] : op(carry.v, incv[i]);
+    if(exclusive) y[i] = h ? init : op(init, before);
+    else y[i] = op(init, incl);
+  }
+  store_thread<T, VT>(out + base + first, valid - first, false, y);
+}
+
+}  // namespace device
+}  // namespace mgpu
