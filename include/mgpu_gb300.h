@@ -75,7 +75,8 @@ typedef struct mgpu_context mgpu_context_t;
  *      vk/context.hxx:11-134, src/vk/context.cxx:15-439) ---- */
 
 /* Creates a context on `device`.  `stream` is a cudaStream_t to enqueue on,
- * or NULL for a stream the context creates and owns. */
+ * or NULL for a non-blocking stream the context creates and owns (pass
+ * cudaStreamLegacy to order work with the legacy default stream). */
 MGPU_API mgpu_status_t mgpu_context_create(int device, void* stream, mgpu_context_t** out);
 MGPU_API mgpu_status_t mgpu_context_destroy(mgpu_context_t* ctx);
 /* Redirects later work to another cudaStream_t (NULL: the owned stream). */
@@ -174,6 +175,22 @@ MGPU_API mgpu_status_t mgpu_segmented_scan(mgpu_context_t* ctx, mgpu_dtype_t typ
   mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,
   const int64_t* offsets, int64_t num_segments, const void* init,
   void* aux_data, size_t* aux_size);
+
+/* ---- CUDA graphs (no reference counterpart; the reference re-records a
+ * Vulkan command buffer per submission, examples/vk_radix/vk_radix.cxx:
+ * 51-63).  Everything enqueued on the context between begin and end is
+ * captured into one executable graph (multi-pass pipelines such as a radix
+ * sort's memset + histogram + passes become one launch).  Calls inside a
+ * capture must pass explicit aux or fit in the context cache already
+ * (see mgpu_cache_reserve); kernel arguments, including counts, are fixed at
+ * capture time. */
+typedef struct mgpu_graph mgpu_graph_t;
+MGPU_API mgpu_status_t mgpu_graph_begin(mgpu_context_t* ctx);
+MGPU_API mgpu_status_t mgpu_graph_end(mgpu_context_t* ctx, mgpu_graph_t** out);
+MGPU_API mgpu_status_t mgpu_graph_launch(mgpu_context_t* ctx, mgpu_graph_t* graph);
+MGPU_API mgpu_status_t mgpu_graph_destroy(mgpu_graph_t* graph);
+/* Grows the context's aux cache to at least `bytes` (stream-ordered). */
+MGPU_API mgpu_status_t mgpu_cache_reserve(mgpu_context_t* ctx, size_t bytes);
 
 /* ---- launch profiling (no reference counterpart; the reference times
  * whole command buffers with clock_gettime, examples/vk_radix/vk_radix.cxx:

@@ -127,3 +127,60 @@ mgpu_status_t mgpu_profile_read(mgpu_context_t* c, char* names, size_t names_byt
 int64_t mgpu_launch_count(mgpu_context_t* c) { return c ? c->ctx.launches : 0; }
 
 }  // extern "C"
+
+// ---- CUDA graphs ----
+
+struct mgpu_graph {
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+};
+
+extern "C" {
+
+mgpu_status_t mgpu_graph_begin(mgpu_context_t* c) {
+  MGPU_CHECK_CTX(c);
+  if(c->ctx.capturing) return MGPU_ERR_INVALID_ARG;
+  if(c->ctx.check(cudaStreamBeginCapture(c->ctx.stream, cudaStreamCaptureModeThreadLocal)))
+    return MGPU_ERR_CUDA;
+  c->ctx.capturing = true;
+  return MGPU_OK;
+}
+
+mgpu_status_t mgpu_graph_end(mgpu_context_t* c, mgpu_graph_t** out) {
+  MGPU_CHECK_CTX(c);
+  if(!out || !c->ctx.capturing) return MGPU_ERR_INVALID_ARG;
+  *out = nullptr;
+  c->ctx.capturing = false;
+  cudaGraph_t g = nullptr;
+  if(c->ctx.check(cudaStreamEndCapture(c->ctx.stream, &g))) return MGPU_ERR_CUDA;
+  mgpu_graph* h = new(std::nothrow) mgpu_graph;
+  if(!h) { cudaGraphDestroy(g); return MGPU_ERR_OOM; }
+  h->device = c->ctx.device;
+  cudaError_t e = cudaGraphInstantiate(&h->exec, g, 0);
+  cudaGraphDestroy(g);
+  if(c->ctx.check(e)) { delete h; return MGPU_ERR_CUDA; }
+  *out = h;
+  return MGPU_OK;
+}
+
+mgpu_status_t mgpu_graph_launch(mgpu_context_t* c, mgpu_graph_t* g) {
+  MGPU_CHECK_CTX(c);
+  if(!g || g->device != c->ctx.device) return MGPU_ERR_INVALID_ARG;
+  return c->ctx.check(cudaGraphLaunch(g->exec, c->ctx.stream)) ? MGPU_ERR_CUDA : MGPU_OK;
+}
+
+mgpu_status_t mgpu_graph_destroy(mgpu_graph_t* g) {
+  if(!g) return MGPU_ERR_INVALID_ARG;
+  cudaSetDevice(g->device);
+  cudaGraphExecDestroy(g->exec);
+  delete g;
+  return MGPU_OK;
+}
+
+mgpu_status_t mgpu_cache_reserve(mgpu_context_t* c, size_t bytes) {
+  MGPU_CHECK_CTX(c);
+  if(c->ctx.capturing) return MGPU_ERR_INVALID_ARG;
+  return c->ctx.cache_allocate(bytes) || !bytes ? MGPU_OK : MGPU_ERR_OOM;
+}
+
+}  // extern "C"

@@ -270,6 +270,9 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   if(reduction && tid == 0 && base + TILE >= count) *reduction = op(s_prefix, tile_agg);
 }
 
+template<typename T>
+__global__ void store_value_kernel(T* p, T v) { *p = v; }
+
 // Device-wide reduce in one launch: each CTA reduces a fixed, strided set of
 // tiles into partials[cta]; the last CTA to finish (ticket counter) reduces
 // the partials in index order.  Deterministic for a given grid size.

@@ -201,6 +201,32 @@ struct seg_small_layout {
   static_assert(warps * slice <= tile, "warp slices fit in the tile buffers");
 };
 
+// Whole sort of at most one tile of keys in one CTA (the single-CTA branch
+// of vk::radix_sort, vk/radix.hxx:221-282, with all bits of the key).
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES>
+__global__ void __launch_bounds__(NT)
+radix_sort_cta(K* keys, V* vals, int n) {
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
+  typedef typename L::U U;
+  constexpr bool HAS_V = L::has_values;
+  extern __shared__ __align__(16) unsigned char smem[];
+  U* ks = (U*)(smem + L::keys_off);
+  V* vs = (V*)(smem + L::vals_off);
+  uint32_t* hist = (uint32_t*)(smem + L::hist_off);
+  uint32_t* tmp = (uint32_t*)(smem + L::tmp_off);
+  const int tid = threadIdx.x;
+  for(int i = tid; i < n; i += NT) {
+    ks[i] = radix_key<K>::to_bits(keys[i]);
+    if constexpr(HAS_V) vs[i] = vals[i];
+  }
+  __syncthreads();
+  group_radix_sort<NT / 32, ITEMS>(ks, vs, n, hist, tmp, PASSES, tid);
+  for(int i = tid; i < n; i += NT) {
+    keys[i] = radix_key<K>::from_bits(ks[i]);
+    if constexpr(HAS_V) vals[i] = vs[i];
+  }
+}
+
 // Persistent sort of every segment up to one tile: CTA-class segments first
 // (whole CTA), then slice-class and warp-class segments (one warp each).
 template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES>

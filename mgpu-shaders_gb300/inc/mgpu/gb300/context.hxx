@@ -103,6 +103,10 @@ struct context_t {
   // that uses it is unaffected.
   void* cache_allocate(size_t bytes) {
     if(bytes > cache_capacity) {
+      if(capturing) {
+        last_error = "aux cache too small during graph capture; reserve it first";
+        return nullptr;
+      }
       if(cache) check(cudaFreeAsync(cache, stream));
       cache = nullptr;
       cache_capacity = 0;
@@ -141,11 +145,12 @@ struct context_t {
   template<typename F>
   status_t launch(const char* name, F&& enqueue) {
     record_t r { name, nullptr, nullptr };
-    if(profiling) { r.begin = acquire_event(); cudaEventRecord(r.begin, stream); }
+    const bool timed = profiling && !capturing;
+    if(timed) { r.begin = acquire_event(); cudaEventRecord(r.begin, stream); }
     enqueue();
     ++launches;
     cudaError_t e = cudaGetLastError();
-    if(profiling) { r.end = acquire_event(); cudaEventRecord(r.end, stream); pending.push_back(r); }
+    if(timed) { r.end = acquire_event(); cudaEventRecord(r.end, stream); pending.push_back(r); }
     return check(e) ? MGPU_ERR_CUDA : MGPU_OK;
   }
 
@@ -190,6 +195,7 @@ struct context_t {
   std::set<void*> host_allocs, device_allocs;
 
   bool profiling = false;
+  bool capturing = false;
   int64_t launches = 0;
   std::vector<record_t> pending;
   std::vector<cudaEvent_t> event_pool;

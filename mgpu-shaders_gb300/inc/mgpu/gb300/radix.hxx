@@ -17,6 +17,7 @@
 
 #include "context.hxx"
 #include "../device/onesweep.cuh"
+#include "../device/segmented.cuh"
 
 namespace mgpu {
 namespace gb300 {
@@ -46,6 +47,20 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
   if(count < 0 || count > radix_max_count) return MGPU_ERR_INVALID_ARG;
 
   int64_t num_tiles = div_up(count, tile);
+  if(num_tiles <= 1) {
+    // One tile: the whole sort runs in shared memory in one CTA; no aux.
+    char* unused = nullptr;
+    status_t s0;
+    if(resolve_aux(ctx, aux_data, aux_size, 0, unused, s0)) return s0;
+    if(count <= 1) return MGPU_OK;
+    if(!keys || (has_values && !vals)) return MGPU_ERR_INVALID_ARG;
+    typedef seg_small_layout<K, V, nt, vt, vt> SL;
+    auto k1 = radix_sort_cta<K, V, nt, vt, vt, passes>;
+    if(!ctx.allow_smem(k1, SL::bytes)) return MGPU_ERR_CUDA;
+    return ctx.launch("radix_sort_cta", [&] {
+      k1<<<1, nt, SL::bytes, ctx.stream>>>(keys, vals, (int)count);
+    });
+  }
   aux_layout_t lay;
   size_t header_off = lay.add(sizeof(uint32_t) * (passes * radix_bins + passes));
   size_t header_bytes = lay.total;

@@ -43,10 +43,10 @@ status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int
   status_t st;
   if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
   if(count == 0) {
-    if(reduction && ctx.check(cudaMemcpyAsync(reduction, &init, sizeof(T),
-      cudaMemcpyHostToDevice, ctx.stream))) return MGPU_ERR_CUDA;
-    if(reduction && ctx.check(cudaStreamSynchronize(ctx.stream))) return MGPU_ERR_CUDA;
-    return MGPU_OK;
+    if(!reduction) return MGPU_OK;
+    return ctx.launch("store_value", [&] {
+      store_value_kernel<T><<<1, 1, 0, ctx.stream>>>(reduction, init);
+    });
   }
   if(!in || !out) return MGPU_ERR_INVALID_ARG;
   if(ctx.check(cudaMemsetAsync(base, 0, lay.total, ctx.stream))) return MGPU_ERR_CUDA;

@@ -22,6 +22,7 @@ DTYPES = {
     np.dtype(np.float64): 5,
 }
 SCAN_TYPES = {"exc": 0, "inc": 1}
+CUDA_STREAM_LEGACY = 0x1    # cudaStreamLegacy: the legacy default stream's handle
 OPS = {"plus": 0, "max": 1, "min": 2}
 COMPS = {"less": 0, "greater": 1}
 
@@ -79,6 +80,10 @@ class Context:
         torch = _torch()
         if stream is None and use_torch_stream:
             stream = torch.cuda.current_stream(device).cuda_stream
+            if stream == 0:
+                # torch's default stream is the legacy NULL stream; NULL at the
+                # C ABI means "create a private stream", so name it explicitly.
+                stream = CUDA_STREAM_LEGACY
         self._h = ctypes.c_void_p()
         _lib.check(lib().mgpu_context_create(device, ctypes.c_void_p(stream), ctypes.byref(self._h)),
                    None)
@@ -115,6 +120,18 @@ class Context:
     @property
     def launch_count(self):
         return lib().mgpu_launch_count(self._h)
+
+    # --- CUDA graphs ---
+    def graph_begin(self):
+        self._check(lib().mgpu_graph_begin(self._h))
+
+    def graph_end(self):
+        g = ctypes.c_void_p()
+        self._check(lib().mgpu_graph_end(self._h, ctypes.byref(g)))
+        return Graph(self, g)
+
+    def cache_reserve(self, nbytes):
+        self._check(lib().mgpu_cache_reserve(self._h, nbytes))
 
     # --- profiling ---
     def profile(self, enable=True):
@@ -230,6 +247,28 @@ class Context:
         self._check(lib().mgpu_transform_saxpy_f32(self._h, ctypes.c_float(a),
                                                    ctypes.c_void_p(x.ptr), ctypes.c_void_p(y.ptr),
                                                    x.count))
+
+
+class Graph:
+    """An executable CUDA graph captured from a context's stream."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self._g = handle
+
+    def launch(self):
+        self.ctx._check(lib().mgpu_graph_launch(self.ctx.handle, self._g))
+
+    def close(self):
+        if self._g:
+            lib().mgpu_graph_destroy(self._g)
+            self._g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def build_dir():

@@ -55,6 +55,11 @@ _SIGS = {
     "mgpu_segmented_sort": ([_VP, _I32, _VP, _I32, _VP, _I64, _VP, _I64, _VP, _SZ], _I32),
     "mgpu_segmented_scan": ([_VP, _I32, _I32, _I32, _VP, _VP, _I64, _VP, _I64, _VP, _VP, _SZ],
                             _I32),
+    "mgpu_graph_begin": ([_VP], _I32),
+    "mgpu_graph_end": ([_VP, _VP], _I32),
+    "mgpu_graph_launch": ([_VP, _VP], _I32),
+    "mgpu_graph_destroy": ([_VP], _I32),
+    "mgpu_cache_reserve": ([_VP, ctypes.c_size_t], _I32),
     "mgpu_profile_enable": ([_VP, _I32], _I32),
     "mgpu_profile_read": ([_VP, _VP, ctypes.c_size_t, _VP, _VP, _I32, _VP], _I32),
     "mgpu_launch_count": ([_VP], _I64),

@@ -146,3 +146,20 @@ def test_radix_full_size_properties(mgpu, ctx, dist):
     assert seen.all()
     eq = gk[1:] == gk[:-1]
     assert np.all(gv[1:][eq] > gv[:-1][eq])
+
+
+def test_radix_orders_with_torch_stream(mgpu, ctx, oracle, rng):
+    """Work enqueued by torch on its current stream (an async device copy)
+    is ordered before the sort: the context enqueues on the same stream."""
+    n = 4_000_037
+    k = gen_keys(rng, n, np.uint32)
+    v = np.arange(n, dtype=np.uint32)
+    src_k, src_v = mgpu.DeviceArray.from_numpy(k), mgpu.DeviceArray.from_numpy(v)
+    dk, dv = mgpu.DeviceArray(n, np.uint32), mgpu.DeviceArray(n, np.uint32)
+    for _ in range(3):
+        dk.copy_from(src_k)          # async on torch's stream
+        dv.copy_from(src_v)
+        ctx.radix_sort(dk, dv)       # no host synchronisation in between
+    ctx.synchronize()
+    ok, ov = oracle.radix_sort(k, v)
+    assert np.array_equal(dk.numpy(), ok) and np.array_equal(dv.numpy(), ov)
