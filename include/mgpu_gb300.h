@@ -176,6 +176,36 @@ MGPU_API mgpu_status_t mgpu_segmented_scan(mgpu_context_t* ctx, mgpu_dtype_t typ
   const int64_t* offsets, int64_t num_segments, const void* init,
   void* aux_data, size_t* aux_size);
 
+/* ---- launch-shape tuning (the reference's (nt, vt[, num_bits]) template
+ * knobs, vk/radix.hxx:195, vk/mergesort.hxx:10, vk/merge.hxx:13,
+ * vk/scan.hxx:10, chosen at run time).  Several shapes of each primitive are
+ * compiled; a per-context table picks one per (primitive, key type, value
+ * width, size bucket = ceil(log2 count)), bucket -1 meaning every size.
+ * The environment variable MGPU_TUNE_FILE names a table loaded at context
+ * creation. */
+typedef enum mgpu_primitive_t {
+  MGPU_PRIM_RADIX = 0,
+  MGPU_PRIM_SCAN = 1,
+  MGPU_PRIM_MERGE = 2,
+  MGPU_PRIM_MERGESORT = 3
+} mgpu_primitive_t;
+/* Number of compiled variants; their names ("<threads>x<items>") are written
+ * '\n'-separated into `names` when it is not NULL. */
+MGPU_API int mgpu_tuning_variants(int primitive, mgpu_dtype_t key_type, char* names,
+  size_t names_bytes);
+MGPU_API mgpu_status_t mgpu_tuning_set(mgpu_context_t* ctx, int primitive,
+  mgpu_dtype_t key_type, int val_bytes, int size_bucket, int variant);
+/* Variant the context would use for this call shape. */
+MGPU_API int mgpu_tuning_get(mgpu_context_t* ctx, int primitive, mgpu_dtype_t key_type,
+  int val_bytes, int64_t count);
+MGPU_API mgpu_status_t mgpu_tuning_save(mgpu_context_t* ctx, const char* path);
+MGPU_API mgpu_status_t mgpu_tuning_load(mgpu_context_t* ctx, const char* path);
+/* Times every variant on device-generated data of this type and size (median
+ * of `reps` runs, each on a fresh unsorted copy; allocates its own scratch)
+ * and records the fastest for the size bucket of `count`. */
+MGPU_API mgpu_status_t mgpu_autotune(mgpu_context_t* ctx, int primitive, mgpu_dtype_t key_type,
+  int val_bytes, int64_t count, int reps, int* best_variant, double* best_ms);
+
 /* ---- CUDA graphs (no reference counterpart; the reference re-records a
  * Vulkan command buffer per submission, examples/vk_radix/vk_radix.cxx:
  * 51-63).  Everything enqueued on the context between begin and end is

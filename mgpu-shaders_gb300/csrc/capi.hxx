@@ -30,3 +30,11 @@ mgpu_status_t dispatch_dtype(mgpu_dtype_t t, F&& f) {
   }
   return MGPU_ERR_INVALID_ARG;
 }
+
+template<typename T> constexpr mgpu_dtype_t dtype_of();
+template<> constexpr mgpu_dtype_t dtype_of<int32_t>() { return MGPU_I32; }
+template<> constexpr mgpu_dtype_t dtype_of<uint32_t>() { return MGPU_U32; }
+template<> constexpr mgpu_dtype_t dtype_of<float>() { return MGPU_F32; }
+template<> constexpr mgpu_dtype_t dtype_of<int64_t>() { return MGPU_I64; }
+template<> constexpr mgpu_dtype_t dtype_of<uint64_t>() { return MGPU_U64; }
+template<> constexpr mgpu_dtype_t dtype_of<double>() { return MGPU_F64; }

@@ -11,6 +11,12 @@ namespace {
 template<typename K, typename V, typename comp_t>
 mgpu_status_t run(mgpu_context* c, const void* ak, const void* av, int64_t an, const void* bk,
   const void* bv, int64_t bn, void* ck, void* cv, void* aux, size_t* aux_size) {
+  int variant = c->ctx.tuning.lookup(prim_merge, (int)dtype_of<K>(), (int)sizeof(V) *
+    !std::is_same<V, no_values>::value, an + bn);
+  constexpr int NT1 = sizeof(K) == 4 ? 256 : 128;
+  if(variant == 1)
+    return merge_kv<NT1, 8>(aux, aux_size, c->ctx, (const K*)ak, (const V*)av, an, (const K*)bk,
+      (const V*)bv, bn, (K*)ck, (V*)cv, comp_t());
   return merge_kv(aux, aux_size, c->ctx, (const K*)ak, (const V*)av, an, (const K*)bk,
     (const V*)bv, bn, (K*)ck, (V*)cv, comp_t());
 }

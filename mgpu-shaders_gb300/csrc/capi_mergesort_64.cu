@@ -12,6 +12,15 @@ mgpu_status_t mergesort_w64(mgpu_context* c, mgpu_dtype_t key_type, void* keys, 
     auto go = [&](auto* vp, auto idx) -> mgpu_status_t {
       typedef std::remove_pointer_t<decltype(vp)> V;
       constexpr bool I = decltype(idx)::value;
+      constexpr int NT1 = sizeof(K) == 4 ? 256 : 128;
+      int variant = c->ctx.tuning.lookup(prim_mergesort, key_type, I ? 4 : val_bytes, count);
+      if(variant == 1) {
+        if(comp == MGPU_LESS)
+          return mergesort_kv<NT1, 8, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+            less_t<K>());
+        return mergesort_kv<NT1, 8, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+          greater_t<K>());
+      }
       if(comp == MGPU_LESS)
         return mergesort_kv<0, 0, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           less_t<K>());

@@ -1,5 +1,5 @@
 // C ABI: mgpu_scan and mgpu_reduce for I32/U32/F32/I64/U64/F64 with plus,
-// max and min.
+// max and min, in every tuned launch-shape variant.
 #include "capi.hxx"
 #include "mgpu/gb300/scan.hxx"
 
@@ -7,19 +7,39 @@ using namespace mgpu::gb300;
 
 namespace {
 
+template<int NT, int VT, typename T, typename op_t>
+mgpu_status_t scan_shape(mgpu_context* c, mgpu_scan_type_t st, const T* in, T* out,
+  int64_t count, T init, T* reduction, void* aux, size_t* aux_size) {
+  if(st == MGPU_SCAN_EXC)
+    return scan<scan_type_exc, NT, VT>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
+      reduction);
+  if(st == MGPU_SCAN_INC)
+    return scan<scan_type_inc, NT, VT>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
+      reduction);
+  return MGPU_ERR_INVALID_ARG;
+}
+
 template<typename T, template<typename> class op_tpl>
 mgpu_status_t run_scan(mgpu_context* c, mgpu_scan_type_t st, const void* in, void* out,
-  int64_t count, const void* init_p, void* reduction, void* aux, size_t* aux_size) {
+  int64_t count, const void* init_p, void* reduction, void* aux, size_t* aux_size, int variant) {
   typedef op_tpl<T> op_t;
   T init = op_t::identity();
   if(init_p) memcpy(&init, init_p, sizeof(T));
-  if(st == MGPU_SCAN_EXC)
-    return scan<scan_type_exc>(aux, aux_size, c->ctx, (const T*)in, count, (T*)out, init,
-      op_t(), (T*)reduction);
-  if(st == MGPU_SCAN_INC)
-    return scan<scan_type_inc>(aux, aux_size, c->ctx, (const T*)in, count, (T*)out, init,
-      op_t(), (T*)reduction);
-  return MGPU_ERR_INVALID_ARG;
+  const T* i = (const T*)in;
+  T* o = (T*)out;
+  T* r = (T*)reduction;
+  if constexpr(sizeof(T) == 4) {
+    switch(variant) {
+      case 1: return scan_shape<256, 8, T, op_t>(c, st, i, o, count, init, r, aux, aux_size);
+      case 2: return scan_shape<512, 16, T, op_t>(c, st, i, o, count, init, r, aux, aux_size);
+      default: return scan_shape<256, 16, T, op_t>(c, st, i, o, count, init, r, aux, aux_size);
+    }
+  } else {
+    switch(variant) {
+      case 1: return scan_shape<512, 8, T, op_t>(c, st, i, o, count, init, r, aux, aux_size);
+      default: return scan_shape<256, 8, T, op_t>(c, st, i, o, count, init, r, aux, aux_size);
+    }
+  }
 }
 
 template<typename T, template<typename> class op_tpl>
@@ -39,15 +59,16 @@ mgpu_status_t mgpu_scan(mgpu_context_t* c, mgpu_dtype_t type, mgpu_scan_type_t s
   mgpu_op_t op, const void* in, void* out, int64_t count, const void* init, void* reduction,
   void* aux_data, size_t* aux_size) {
   MGPU_CHECK_CTX(c);
+  int variant = c->ctx.tuning.lookup(prim_scan, type, 0, count);
   return dispatch_dtype(type, [&](auto* tp) -> mgpu_status_t {
     typedef std::remove_pointer_t<decltype(tp)> T;
     switch(op) {
       case MGPU_PLUS: return run_scan<T, plus_t>(c, scan_type, in, out, count, init, reduction,
-        aux_data, aux_size);
+        aux_data, aux_size, variant);
       case MGPU_MAX: return run_scan<T, maximum_t>(c, scan_type, in, out, count, init, reduction,
-        aux_data, aux_size);
+        aux_data, aux_size, variant);
       case MGPU_MIN: return run_scan<T, minimum_t>(c, scan_type, in, out, count, init, reduction,
-        aux_data, aux_size);
+        aux_data, aux_size, variant);
     }
     return MGPU_ERR_INVALID_ARG;
   });

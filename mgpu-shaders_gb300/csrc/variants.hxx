@@ -1,0 +1,39 @@
+// Compiled launch-shape variants of each primitive, selected at run time by
+// the context's tuning table (mgpu/gb300/tuning.hxx).  Variant 0 is the
+// default.  Names are "<threads>x<items per thread>".
+#pragma once
+
+#include "mgpu_gb300.h"
+
+namespace variants {
+
+// radix_sort: 4-byte keys {256x16 (3 CTAs/SM), 512x16 (2), 256x12 (4)};
+// 8-byte keys {256x12 (3), 256x8 (4)}.
+inline int radix_count(int key_bytes) { return key_bytes == 4 ? 3 : 2; }
+inline const char* radix_name(int key_bytes, int v) {
+  static const char* n4[] = { "256x16", "512x16", "256x12" };
+  static const char* n8[] = { "256x12", "256x8" };
+  return key_bytes == 4 ? n4[v] : n8[v];
+}
+
+// scan / reduce: 4-byte {256x16, 256x8, 512x16}; 8-byte {256x8, 512x8}.
+inline int scan_count(int bytes) { return bytes == 4 ? 3 : 2; }
+inline const char* scan_name(int bytes, int v) {
+  static const char* n4[] = { "256x16", "256x8", "512x16" };
+  static const char* n8[] = { "256x8", "512x8" };
+  return bytes == 4 ? n4[v] : n8[v];
+}
+
+// merge / mergesort: 4-byte keys {256x16, 256x8}; 8-byte keys {256x8, 128x8}.
+inline int merge_count(int) { return 2; }
+inline const char* merge_name(int bytes, int v) {
+  static const char* n4[] = { "256x16", "256x8" };
+  static const char* n8[] = { "256x8", "128x8" };
+  return bytes == 4 ? n4[v] : n8[v];
+}
+
+inline int dtype_bytes(mgpu_dtype_t t) {
+  return (t == MGPU_I64 || t == MGPU_U64 || t == MGPU_F64) ? 8 : 4;
+}
+
+}  // namespace variants

@@ -107,8 +107,8 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
   uint32_t* tmp, int passes, int gtid) {
   constexpr bool HAS_V = !std::is_same<V, no_values>::value;
   constexpr int G = 32 * W;
-  constexpr int DPT = radix_bins / G;          // digits per thread
-  static_assert(radix_bins % G == 0, "group size divides 256");
+  constexpr int DPT = G >= radix_bins ? 1 : radix_bins / G;   // digits per thread
+  static_assert(G >= radix_bins ? G % radix_bins == 0 : radix_bins % G == 0, "group size");
   const int lane = gtid & 31, gw = gtid >> 5;
   const int warp_base = gw * 32 * ITEMS;
   const int rem = n - warp_base - lane;
@@ -146,10 +146,12 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
     for(int j = 0; j < DPT; ++j) {
       int d = gtid * DPT + j;
       uint32_t t = 0;
-      for(int w = 0; w < W; ++w) {
-        uint32_t c = hist[w * radix_bins + d];
-        hist[w * radix_bins + d] = t;
-        t += c;
+      if(d < radix_bins) {
+        for(int w = 0; w < W; ++w) {
+          uint32_t c = hist[w * radix_bins + d];
+          hist[w * radix_bins + d] = t;
+          t += c;
+        }
       }
       tot[j] = t;
       sum += t;
@@ -170,7 +172,8 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
 #pragma unroll
     for(int j = 0; j < DPT; ++j) {
       int d = gtid * DPT + j;
-      for(int w = 0; w < W; ++w) hist[w * radix_bins + d] += excl;
+      if(d < radix_bins)
+        for(int w = 0; w < W; ++w) hist[w * radix_bins + d] += excl;
       excl += tot[j];
     }
     gsync();

@@ -20,6 +20,8 @@
 #include <vector>
 
 #include "mgpu_gb300.h"
+#include "tuning.hxx"
+#include <cstdlib>
 
 namespace mgpu {
 namespace gb300 {
@@ -44,6 +46,7 @@ struct context_t {
     if(check(cudaMalloc(&d_error, sizeof(int)))) { init_status = MGPU_ERR_OOM; return; }
     if(check(cudaMemsetAsync(d_error, 0, sizeof(int), stream))) { init_status = MGPU_ERR_CUDA; return; }
     check(cudaStreamSynchronize(stream));
+    if(const char* path = getenv("MGPU_TUNE_FILE")) tuning.load(path);
   }
 
   ~context_t() {
@@ -194,6 +197,7 @@ struct context_t {
   size_t cache_capacity = 0;
   std::set<void*> host_allocs, device_allocs;
 
+  tuning_table_t tuning;
   bool profiling = false;
   bool capturing = false;
   int64_t launches = 0;

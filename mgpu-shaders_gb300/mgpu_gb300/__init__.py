@@ -22,6 +22,7 @@ DTYPES = {
     np.dtype(np.float64): 5,
 }
 SCAN_TYPES = {"exc": 0, "inc": 1}
+PRIMITIVES = {"radix": 0, "scan": 1, "merge": 2, "mergesort": 3}
 CUDA_STREAM_LEGACY = 0x1    # cudaStreamLegacy: the legacy default stream's handle
 OPS = {"plus": 0, "max": 1, "min": 2}
 COMPS = {"less": 0, "greater": 1}
@@ -120,6 +121,34 @@ class Context:
     @property
     def launch_count(self):
         return lib().mgpu_launch_count(self._h)
+
+    # --- launch-shape tuning ---
+    def tuning_variants(self, primitive, key_dtype):
+        buf = ctypes.create_string_buffer(512)
+        n = lib().mgpu_tuning_variants(PRIMITIVES[primitive], DTYPES[np.dtype(key_dtype)], buf, 512)
+        return buf.value.decode().split("\n")[:n]
+
+    def tuning_set(self, primitive, key_dtype, val_bytes, bucket, variant):
+        self._check(lib().mgpu_tuning_set(self._h, PRIMITIVES[primitive],
+                                          DTYPES[np.dtype(key_dtype)], val_bytes, bucket, variant))
+
+    def tuning_get(self, primitive, key_dtype, val_bytes, count):
+        return lib().mgpu_tuning_get(self._h, PRIMITIVES[primitive], DTYPES[np.dtype(key_dtype)],
+                                     val_bytes, count)
+
+    def tuning_save(self, path):
+        self._check(lib().mgpu_tuning_save(self._h, path.encode()))
+
+    def tuning_load(self, path):
+        self._check(lib().mgpu_tuning_load(self._h, path.encode()))
+
+    def autotune(self, primitive, key_dtype, val_bytes, count, reps=3):
+        best = ctypes.c_int()
+        ms = ctypes.c_double()
+        self._check(lib().mgpu_autotune(self._h, PRIMITIVES[primitive],
+                                        DTYPES[np.dtype(key_dtype)], val_bytes, count, reps,
+                                        ctypes.byref(best), ctypes.byref(ms)))
+        return best.value, ms.value
 
     # --- CUDA graphs ---
     def graph_begin(self):

@@ -55,6 +55,12 @@ _SIGS = {
     "mgpu_segmented_sort": ([_VP, _I32, _VP, _I32, _VP, _I64, _VP, _I64, _VP, _SZ], _I32),
     "mgpu_segmented_scan": ([_VP, _I32, _I32, _I32, _VP, _VP, _I64, _VP, _I64, _VP, _VP, _SZ],
                             _I32),
+    "mgpu_tuning_variants": ([_I32, _I32, _VP, ctypes.c_size_t], _I32),
+    "mgpu_tuning_set": ([_VP, _I32, _I32, _I32, _I32, _I32], _I32),
+    "mgpu_tuning_get": ([_VP, _I32, _I32, _I32, _I64], _I32),
+    "mgpu_tuning_save": ([_VP, ctypes.c_char_p], _I32),
+    "mgpu_tuning_load": ([_VP, ctypes.c_char_p], _I32),
+    "mgpu_autotune": ([_VP, _I32, _I32, _I32, _I64, _I32, _VP, _VP], _I32),
     "mgpu_graph_begin": ([_VP], _I32),
     "mgpu_graph_end": ([_VP, _VP], _I32),
     "mgpu_graph_launch": ([_VP, _VP], _I32),
