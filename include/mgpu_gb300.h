@@ -141,6 +141,24 @@ MGPU_API mgpu_status_t mgpu_scan(mgpu_context_t* ctx, mgpu_dtype_t type, mgpu_sc
   mgpu_op_t op, const void* in, void* out, int64_t count, const void* init,
   void* reduction, void* aux_data, size_t* aux_size);
 
+/* ---- scan without any allocation.  No counterpart in the reference: it is
+ * an addition for callers that cannot allocate device memory (an operator
+ * inside another engine that owns all device memory, a plugin whose enqueue
+ * must not allocate or synchronise, a pipeline that forbids allocation after
+ * start-up).  Same results as mgpu_scan for I32/U32/F32 (plus, max, min;
+ * exclusive or inclusive), enqueued on `stream` (a cudaStream_t, NULL = the
+ * legacy default stream) on the current device, with no context.  Its
+ * scratch is a fixed 512 KiB array inside the library, held on every GPU that
+ * loads it until exit; counts above MGPU_SCAN_NOALLOC_MAX_COUNT return
+ * MGPU_ERR_INVALID_ARG, 8-byte types MGPU_ERR_UNSUPPORTED.  The first call on
+ * a device looks up that array's device address; make it outside any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so
+ * order them (for example, on one stream). */
+#define MGPU_SCAN_NOALLOC_MAX_COUNT (1LL << 28)
+MGPU_API mgpu_status_t mgpu_scan_noalloc(void* stream, mgpu_dtype_t type,
+  mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,
+  const void* init, void* reduction);
+
 /* ---- reduce (cta_reduce_t, common/cta_scan.hxx:9-59, as a device-wide
  * primitive).  Writes init (+) all inputs to the device pointer `out`. */
 MGPU_API mgpu_status_t mgpu_reduce(mgpu_context_t* ctx, mgpu_dtype_t type, mgpu_op_t op,

@@ -1,0 +1,123 @@
+// mgpu_scan_noalloc: the single-pass look-back scan for callers that cannot
+// allocate device memory.
+//
+// Who needs it: code that runs where allocation is not allowed or not
+// possible, for example an operator inside another framework's engine that
+// owns all device memory through its own allocator, a plugin whose enqueue
+// hook must not allocate (cudaMalloc can synchronise the device and breaks
+// stream capture), or a real-time pipeline that forbids allocation after
+// start-up.  mgpu_scan needs a context (which allocates its error word and
+// may allocate its aux cache) or caller-provided aux; this entry point needs
+// neither.
+//
+// Its scratch (tile counter, error word, one 64-bit look-back status word per
+// 4096-element tile) lives in the file-scope array below, sized for at most
+// MGPU_SCAN_NOALLOC_MAX_COUNT elements: 65,538 words = 512 KiB + 16 bytes.
+// Every GPU that loads this library holds that array until the process exits.
+// All calls share it, and it keeps the last call's contents: each call clears
+// the counter, the error word and the status words it will use before its
+// kernel runs.  Calls whose work overlaps on the GPU (different streams, or
+// different host threads, on the same device) race on the array; callers must
+// order them, for example by issuing them on one stream.
+//
+// The array's host-side name is only a stand-in, not a device address; the
+// device address comes from cudaGetSymbolAddress, called once per device with
+// that device current, the first time this entry point runs on it.  Make that
+// first call outside any stream capture.
+#include "mgpu_gb300.h"
+#include "mgpu/device/scan.cuh"
+
+#include <mutex>
+
+namespace {
+
+using namespace mgpu::device;
+
+constexpr int kThreads = 256;
+constexpr int kItems = 16;
+constexpr int64_t kTile = (int64_t)kThreads * kItems;
+constexpr int64_t kMaxTiles = MGPU_SCAN_NOALLOC_MAX_COUNT / kTile;
+constexpr int kMaxDevices = 64;
+static_assert(MGPU_SCAN_NOALLOC_MAX_COUNT % kTile == 0, "whole tiles");
+
+// Word 0: tile counter (low 32 bits).  Word 1: device error word.
+// Words 2 .. 2 + kMaxTiles: look-back status of each tile.
+static __device__ __align__(256) uint64_t g_noalloc_scan_scratch[2 + kMaxTiles];
+
+std::mutex g_setup_mutex;
+uint64_t* g_scratch_address[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (set up once).
+cudaError_t scratch_address(int device, uint64_t** out) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if(!g_scratch_address[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+    if(e != cudaSuccess) return e;
+    g_scratch_address[device] = (uint64_t*)p;
+  }
+  *out = g_scratch_address[device];
+  return cudaSuccess;
+}
+
+template<typename T, typename op_t>
+mgpu_status_t launch(cudaStream_t stream, mgpu_scan_type_t scan_type, const void* in, void* out,
+  int64_t count, const void* init_p, void* reduction, uint64_t* scratch) {
+  T init = op_t::identity();
+  if(init_p) memcpy(&init, init_p, sizeof(T));
+  if(count == 0) {
+    if(reduction) store_value_kernel<T><<<1, 1, 0, stream>>>((T*)reduction, init);
+    return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+  }
+  const int64_t num_tiles = div_up(count, kTile);
+  if(cudaMemsetAsync(scratch, 0, sizeof(uint64_t) * (2 + num_tiles), stream) != cudaSuccess)
+    return MGPU_ERR_CUDA;
+  tile_status_t<T> status;
+  status.bind(scratch + 2, num_tiles);
+  uint32_t* counter = (uint32_t*)scratch;
+  int* error = (int*)(scratch + 1);
+  int vec = 0 == (((uintptr_t)in | (uintptr_t)out) & 15);
+  if(scan_type == MGPU_SCAN_EXC)
+    scan_kernel<T, op_t, kThreads, kItems, true><<<(unsigned)num_tiles, kThreads, 0, stream>>>(
+      (const T*)in, (T*)out, count, init, op_t(), status, counter, (T*)reduction, error, vec);
+  else
+    scan_kernel<T, op_t, kThreads, kItems, false><<<(unsigned)num_tiles, kThreads, 0, stream>>>(
+      (const T*)in, (T*)out, count, init, op_t(), status, counter, (T*)reduction, error, vec);
+  return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+}
+
+template<typename T>
+mgpu_status_t by_op(mgpu_op_t op, cudaStream_t s, mgpu_scan_type_t st, const void* in,
+  void* out, int64_t count, const void* init, void* red, uint64_t* scratch) {
+  switch(op) {
+    case MGPU_PLUS: return launch<T, plus_t<T>>(s, st, in, out, count, init, red, scratch);
+    case MGPU_MAX: return launch<T, max_t<T>>(s, st, in, out, count, init, red, scratch);
+    case MGPU_MIN: return launch<T, min_t<T>>(s, st, in, out, count, init, red, scratch);
+  }
+  return MGPU_ERR_INVALID_ARG;
+}
+
+}  // namespace
+
+extern "C" mgpu_status_t mgpu_scan_noalloc(void* stream, mgpu_dtype_t type,
+  mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,
+  const void* init, void* reduction) {
+  if(count < 0 || count > MGPU_SCAN_NOALLOC_MAX_COUNT) return MGPU_ERR_INVALID_ARG;
+  if(scan_type != MGPU_SCAN_EXC && scan_type != MGPU_SCAN_INC) return MGPU_ERR_INVALID_ARG;
+  if(op != MGPU_PLUS && op != MGPU_MAX && op != MGPU_MIN) return MGPU_ERR_INVALID_ARG;
+  if(type != MGPU_I32 && type != MGPU_U32 && type != MGPU_F32) return MGPU_ERR_UNSUPPORTED;
+  if(count > 0 && (!in || !out)) return MGPU_ERR_INVALID_ARG;
+  int device = 0;
+  if(cudaGetDevice(&device) != cudaSuccess) return MGPU_ERR_CUDA;
+  if(device < 0 || device >= kMaxDevices) return MGPU_ERR_UNSUPPORTED;
+  uint64_t* scratch = nullptr;
+  if(scratch_address(device, &scratch) != cudaSuccess) return MGPU_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch(type) {
+    case MGPU_I32: return by_op<int32_t>(op, s, scan_type, in, out, count, init, reduction, scratch);
+    case MGPU_U32: return by_op<uint32_t>(op, s, scan_type, in, out, count, init, reduction, scratch);
+    case MGPU_F32: return by_op<float>(op, s, scan_type, in, out, count, init, reduction, scratch);
+    default: break;
+  }
+  return MGPU_ERR_UNSUPPORTED;
+}
