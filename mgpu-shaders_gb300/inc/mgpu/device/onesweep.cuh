@@ -14,12 +14,14 @@
 //  * onesweep_pass: one launch per digit.  Each CTA takes the next tile id
 //    from an atomic counter (so every predecessor tile is already resident),
 //    bulk-copies its keys and values into shared memory with the TMA engine,
-//    ranks digits per warp with match.any (stable: rows of 32 lanes in
-//    element order), publishes its per-digit counts, then walks back over
-//    predecessor tiles' published counts (decoupled look-back) to find its
-//    global offset per digit.  Keys and values are scattered to shared memory
-//    in local digit order and written out in runs, so global stores coalesce.
-//    Per pass the kernel reads and writes each key and value once.
+//    ranks digits per warp (peer lanes found with one ballot per digit bit;
+//    stable: rows of 32 lanes in element order), publishes its per-digit
+//    counts, then walks back over predecessor tiles' published counts
+//    (decoupled look-back, several predecessors per L2 round trip, the first
+//    round overlapping the shared-memory scatter) to find its global offset
+//    per digit.  Keys and values are scattered to shared memory in local digit
+//    order and written out in runs, so global stores coalesce.  Per pass the
+//    kernel reads and writes each key and value once.
 //
 // The look-back status of (tile, digit) is one 32-bit word: two flag bits
 // (aggregate / inclusive prefix) over a 30-bit count, hence count < 2^30.
@@ -57,16 +59,22 @@ struct onesweep_args {
   int tma;                   // pointers allow 16-byte bulk copies
 };
 
-template<typename K, typename V, int NT, int ITEMS>
+// CHAINS: each warp ranks its ITEMS rows as CHAINS independent chains of
+// consecutive rows, each with its own digit counters, so the chains' shared-
+// memory dependencies overlap; chain offsets are folded in afterwards.
+template<typename K, typename V, int NT, int ITEMS, int CHAINS = 1>
 struct onesweep_layout {
   typedef typename radix_key<K>::bits_t U;
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
   static constexpr int tile = NT * ITEMS;
   static constexpr int num_warps = NT / 32;
+  static constexpr int chains = CHAINS;
   static constexpr size_t keys_off = 0;
   static constexpr size_t vals_off = keys_off + sizeof(U) * tile;
   static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
-  static constexpr size_t gbase_off = hist_off + sizeof(uint32_t) * num_warps * radix_bins;
+  static constexpr size_t gbase_off =
+    hist_off + sizeof(uint32_t) * num_warps * CHAINS * radix_bins;
+  static_assert(ITEMS % CHAINS == 0, "chains split the rows evenly");
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
   static constexpr size_t tile_off = bar_off + sizeof(uint64_t) * 2;
@@ -146,9 +154,9 @@ struct onesweep_tile_t {
 
 // Claims the next tile id and prepares shared memory (barrier, counters).
 // Returns the tile id; every thread of the CTA must call it.
-template<typename K, typename V, int NT, int ITEMS>
+template<typename K, typename V, int NT, int ITEMS, int CHAINS = 1>
 __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned char* smem) {
-  typedef onesweep_layout<K, V, NT, ITEMS> L;
+  typedef onesweep_layout<K, V, NT, ITEMS, CHAINS> L;
   uint32_t* whist = (uint32_t*)(smem + L::hist_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
   int* s_tile = (int*)(smem + L::tile_off);
@@ -158,15 +166,88 @@ __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned c
     mbar_init(bar, 1);
     fence_mbar_init();
   }
-  for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
+  for(int i = tid; i < L::num_warps * CHAINS * radix_bins; i += NT) whist[i] = 0;
   __syncthreads();
   return *s_tile;
 }
 
-template<typename K, typename V, int NT, int ITEMS>
+// Peers of this lane in the warp: lanes whose 8-bit digit equals `d`, found
+// with one ballot per digit bit (the reference's get_matching_lanes,
+// common/cta_radix.hxx:242-256; much cheaper than match.any here).
+__device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
+  uint32_t m = 0xffffffffu;
+#pragma unroll
+  for(int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t v = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+}
+
+// Decoupled look-back of one digit: the sum of the counts of all predecessor
+// tiles.  `pred` is this digit's word in the nearest predecessor's row; there
+// are `num_pred` predecessors, 256 words apart.  Each round loads the status
+// of WINDOW predecessors at once (one L2 round trip) and consumes them in
+// order: aggregates are added, an inclusive prefix ends the walk, and an
+// unpublished status stops the round (the walk resumes there).  issue()
+// starts the first round early so its latency overlaps other work; finish()
+// completes the walk.  Bounded.
+template<int WINDOW>
+struct lookback_window_t {
+  uint32_t s[WINDOW];
+  const uint32_t* pred;
+  int left;
+
+  __device__ __forceinline__ void load() {
+#pragma unroll
+    for(int k = 0; k < WINDOW; ++k)
+      s[k] = k < left ? ld_relaxed(pred - k * radix_bins) : lb_inc;
+  }
+  __device__ __forceinline__ void issue(const uint32_t* p, int num_pred) {
+    pred = p;
+    left = num_pred;
+    load();
+  }
+  __device__ __forceinline__ uint32_t finish(int* error) {
+    uint32_t excl = 0;
+    int spins = 0;
+    while(true) {
+      int used = 0;
+      bool done = false, stalled = false;
+#pragma unroll
+      for(int k = 0; k < WINDOW; ++k) {
+        if(!done && !stalled) {
+          uint32_t flag = s[k] & ~lb_count;
+          if(!flag) {
+            stalled = true;
+          } else {
+            excl += s[k] & lb_count;
+            ++used;
+            done = flag == lb_inc;
+          }
+        }
+      }
+      if(done) return excl;
+      pred -= used * radix_bins;
+      left -= used;
+      if(stalled) {
+        ++spins;
+        if(spins >= spin_limit ||
+           (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
+          raise_error(error, err_lookback_timeout);
+          return excl;
+        }
+      }
+      load();
+    }
+  }
+};
+
+template<typename K, typename V, int NT, int ITEMS, int WINDOW = 4, int CHAINS = 1>
 __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const onesweep_tile_t& t, unsigned char* smem) {
-  typedef onesweep_layout<K, V, NT, ITEMS> L;
+  typedef onesweep_layout<K, V, NT, ITEMS, CHAINS> L;
   typedef typename L::U U;
   constexpr int TILE = L::tile;
   constexpr int NWARPS = L::num_warps;
@@ -231,19 +312,29 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   // Warp-level stable ranking: item i of every lane forms one row; lanes
   // holding equal digits are peers.  The rank counts earlier rows and lower
   // lanes of the same row (element order), via a per-warp digit counter.
+  // Chain c covers rows [c * RPC, (c + 1) * RPC) with counters
+  // whist[warp][c][256]; one step advances every chain by one row.
+  constexpr int RPC = ITEMS / CHAINS;
   uint32_t r[ITEMS];
-  uint32_t* wh = whist + warp * radix_bins;
+  uint32_t* wh = whist + warp * CHAINS * radix_bins;
   const uint32_t lt_mask = lanemask_lt();
 #pragma unroll
-  for(int i = 0; i < ITEMS; ++i) {
-    uint32_t d = extract_digit(k[i], a.shift, 8);
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
-    uint32_t below = peers & lt_mask;
-    uint32_t cnt = wh[d];
+  for(int step = 0; step < RPC; ++step) {
+    uint32_t d[CHAINS], peers[CHAINS], cnt[CHAINS];
+#pragma unroll
+    for(int c = 0; c < CHAINS; ++c) {
+      d[c] = extract_digit(k[c * RPC + step], a.shift, 8);
+      peers[c] = match_digit8(d[c]);
+      cnt[c] = wh[c * radix_bins + d[c]];
+    }
     __syncwarp();
-    if(!below) wh[d] = cnt + __popc(peers);
+#pragma unroll
+    for(int c = 0; c < CHAINS; ++c) {
+      uint32_t below = peers[c] & lt_mask;
+      if(!below) wh[c * radix_bins + d[c]] = cnt[c] + __popc(peers[c]);
+      r[c * RPC + step] = cnt[c] + __popc(below);
+    }
     __syncwarp();
-    r[i] = cnt + __popc(below);
   }
   __syncthreads();
 
@@ -253,7 +344,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   uint32_t tile_cnt = 0, glob_cnt = 0, valid_cnt = 0;
   if(tid < radix_bins) {
 #pragma unroll 4
-    for(int w = 0; w < NWARPS; ++w) {
+    for(int w = 0; w < NWARPS * CHAINS; ++w) {
       uint32_t c = whist[w * radix_bins + tid];
       whist[w * radix_bins + tid] = tile_cnt;
       tile_cnt += c;
@@ -265,32 +356,13 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   uint32_t tile_start = tile_cnt, glob_start = glob_cnt;
   scan_256_pair(tile_start, glob_start, stmp);
 
+  // Issue the first look-back window now; its L2 round trip overlaps the
+  // shared-memory scatter below.
+  lookback_window_t<WINDOW> lbw;
   if(tid < radix_bins) {
-    uint32_t excl = 0;
-    if(tile > 0) {
-      const uint32_t* pred = t.lb_row + tid - radix_bins;
-      int spins = 0;
-      while(true) {
-        uint32_t s = ld_relaxed(pred);
-        uint32_t flag = s & ~lb_count;
-        if(!flag) {
-          ++spins;
-          if(spins >= spin_limit ||
-             (0 == (spins & (spin_poll_error - 1)) && error_raised(a.error))) {
-            raise_error(a.error, err_lookback_timeout);
-            break;
-          }
-          continue;
-        }
-        excl += s & lb_count;
-        if(flag == lb_inc) break;
-        pred -= radix_bins;
-      }
-      st_relaxed(&t.lb_row[tid], lb_inc | (excl + valid_cnt));
-    }
-    gbase[tid] = (int)(glob_start + excl - tile_start);
+    if(tile > 0) lbw.issue(t.lb_row + tid - radix_bins, tile);
 #pragma unroll 4
-    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] += tile_start;
+    for(int w = 0; w < NWARPS * CHAINS; ++w) whist[w * radix_bins + tid] += tile_start;
   }
   __syncthreads();
 
@@ -299,7 +371,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 #pragma unroll
   for(int i = 0; i < ITEMS; ++i) {
     uint32_t d = extract_digit(k[i], a.shift, 8);
-    r[i] += wh[d];
+    r[i] += wh[(i / RPC) * radix_bins + d];
     ks[r[i]] = k[i];
   }
   if constexpr(HAS_V) {
@@ -316,37 +388,58 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) vs[r[i]] = v[i];
   }
+
+  // Finish the look-back, publish the inclusive prefix, and form each
+  // digit's global base (global digit start + predecessors - local start).
+  if(tid < radix_bins) {
+    uint32_t excl = 0;
+    if(tile > 0) {
+      excl = lbw.finish(a.error);
+      st_relaxed(&t.lb_row[tid], lb_inc | (excl + valid_cnt));
+    }
+    gbase[tid] = (int)(glob_start + excl - tile_start);
+  }
   __syncthreads();
 
   // Write out in local order: consecutive threads hit consecutive addresses
-  // inside each digit's run.
+  // inside each digit's run.  Loads first, then stores, for memory-level
+  // parallelism.
   const int out_rem = valid - tid;
   U* keys_out = a.keys_out + t.out_base;
   V* vals_out = a.vals_out + t.out_base;
+  U u[ITEMS];
+  uint32_t dst[ITEMS];
 #pragma unroll
   for(int j = 0; j < ITEMS; ++j) {
     int idx = j * NT + tid;
+    u[j] = j * NT < out_rem ? ks[idx] : 0;
+    dst[j] = (uint32_t)gbase[extract_digit(u[j], a.shift, 8)] + idx;
+  }
+#pragma unroll
+  for(int j = 0; j < ITEMS; ++j) {
     if(j * NT < out_rem) {
-      U u = ks[idx];
-      uint32_t d = extract_digit(u, a.shift, 8);
-      uint32_t dst = (uint32_t)gbase[d] + idx;
       if(a.last) {
-        K key = radix_key<K>::from_bits(u);
-        memcpy(&keys_out[dst], &key, sizeof(K));
+        K key = radix_key<K>::from_bits(u[j]);
+        memcpy(&keys_out[dst[j]], &key, sizeof(K));
       } else {
-        keys_out[dst] = u;
+        keys_out[dst[j]] = u[j];
       }
-      if constexpr(HAS_V) vals_out[dst] = vs[idx];
     }
+  }
+  if constexpr(HAS_V) {
+#pragma unroll
+    for(int j = 0; j < ITEMS; ++j)
+      if(j * NT < out_rem) vals_out[dst[j]] = vs[j * NT + tid];
   }
 }
 
-template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS>
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int WINDOW = 4,
+  int CHAINS = 1>
 __global__ void __launch_bounds__(NT, MIN_BLOCKS)
 onesweep_pass(onesweep_args<K, V> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int TILE = NT * ITEMS;
-  const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
+  const int tile = onesweep_begin<K, V, NT, ITEMS, CHAINS>(a.tile_counter, smem);
   onesweep_tile_t t;
   t.base = (int64_t)tile * TILE;
   t.valid = (int)min((int64_t)TILE, a.count - t.base);
@@ -354,7 +447,7 @@ onesweep_pass(onesweep_args<K, V> a) {
   t.lb_row = a.lookback + (int64_t)tile * radix_bins;
   t.hist = a.hist;
   t.out_base = 0;
-  onesweep_tile<K, V, NT, ITEMS>(a, t, smem);
+  onesweep_tile<K, V, NT, ITEMS, WINDOW, CHAINS>(a, t, smem);
 }
 
 }  // namespace device

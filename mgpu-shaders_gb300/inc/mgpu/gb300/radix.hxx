@@ -24,7 +24,7 @@ namespace gb300 {
 
 // Default tile shapes per key width (threads, keys per thread, CTAs per SM).
 template<int key_bytes> struct radix_tuning;
-template<> struct radix_tuning<4> { enum { nt = 256, vt = 16, min_blocks = 3 }; };
+template<> struct radix_tuning<4> { enum { nt = 512, vt = 16, min_blocks = 2 }; };
 template<> struct radix_tuning<8> { enum { nt = 256, vt = 12, min_blocks = 3 }; };
 
 // Largest count the 30-bit look-back status word can carry.
