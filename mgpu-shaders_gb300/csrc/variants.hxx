@@ -7,11 +7,11 @@
 
 namespace variants {
 
-// radix_sort: 4-byte keys {512x16 (2 CTAs/SM), 256x16 (3), 256x12 (4)};
+// radix_sort: 4-byte keys {256x20 (3 CTAs/SM), 512x16 (2), 256x16 (3)};
 // 8-byte keys {256x12 (3), 256x8 (4)}.
 inline int radix_count(int key_bytes) { return key_bytes == 4 ? 3 : 2; }
 inline const char* radix_name(int key_bytes, int v) {
-  static const char* n4[] = { "512x16", "256x16", "256x12" };
+  static const char* n4[] = { "256x20", "512x16", "256x16" };
   static const char* n8[] = { "256x12", "256x8" };
   return key_bytes == 4 ? n4[v] : n8[v];
 }

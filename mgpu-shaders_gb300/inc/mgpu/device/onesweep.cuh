@@ -59,26 +59,23 @@ struct onesweep_args {
   int tma;                   // pointers allow 16-byte bulk copies
 };
 
-// CHAINS: each warp ranks its ITEMS rows as CHAINS independent chains of
-// consecutive rows, each with its own digit counters, so the chains' shared-
-// memory dependencies overlap; chain offsets are folded in afterwards.
-template<typename K, typename V, int NT, int ITEMS, int CHAINS = 1>
+template<typename K, typename V, int NT, int ITEMS>
 struct onesweep_layout {
   typedef typename radix_key<K>::bits_t U;
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
   static constexpr int tile = NT * ITEMS;
   static constexpr int num_warps = NT / 32;
-  static constexpr int chains = CHAINS;
   static constexpr size_t keys_off = 0;
   static constexpr size_t vals_off = keys_off + sizeof(U) * tile;
   static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
-  static constexpr size_t gbase_off =
-    hist_off + sizeof(uint32_t) * num_warps * CHAINS * radix_bins;
-  static_assert(ITEMS % CHAINS == 0, "chains split the rows evenly");
+  static constexpr size_t gbase_off = hist_off + sizeof(uint32_t) * num_warps * radix_bins;
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
   static constexpr size_t tile_off = bar_off + sizeof(uint64_t) * 2;
   static constexpr size_t bytes = tile_off + 16;
+  // Each warp's slice of the key buffer (32 * ITEMS keys) doubles as its two
+  // banks of 256 match masks while it ranks, when it is large enough.
+  static constexpr bool match_in_slice = sizeof(U) * 32 * ITEMS >= 2 * 256 * sizeof(uint32_t);
   static_assert(NT >= radix_bins && NT % 32 == 0, "one thread per digit");
   static_assert((sizeof(U) * tile) % 16 == 0, "bulk-copy granularity");
 };
@@ -154,9 +151,9 @@ struct onesweep_tile_t {
 
 // Claims the next tile id and prepares shared memory (barrier, counters).
 // Returns the tile id; every thread of the CTA must call it.
-template<typename K, typename V, int NT, int ITEMS, int CHAINS = 1>
+template<typename K, typename V, int NT, int ITEMS>
 __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned char* smem) {
-  typedef onesweep_layout<K, V, NT, ITEMS, CHAINS> L;
+  typedef onesweep_layout<K, V, NT, ITEMS> L;
   uint32_t* whist = (uint32_t*)(smem + L::hist_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
   int* s_tile = (int*)(smem + L::tile_off);
@@ -166,23 +163,29 @@ __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned c
     mbar_init(bar, 1);
     fence_mbar_init();
   }
-  for(int i = tid; i < L::num_warps * CHAINS * radix_bins; i += NT) whist[i] = 0;
+  for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
   __syncthreads();
   return *s_tile;
 }
 
-// Peers of this lane in the warp: lanes whose 8-bit digit equals `d`, found
-// with one ballot per digit bit (the reference's get_matching_lanes,
-// common/cta_radix.hxx:242-256; much cheaper than match.any here).
-__device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
-  uint32_t m = 0xffffffffu;
+// Peers of this lane in the warp (lanes whose 8-bit digit equals its own),
+// found with one ballot per digit bit, as the reference's get_matching_lanes
+// (common/cta_radix.hxx:242-256) does; used where no shared-memory match
+// masks fit.  The digit sits at bit offset `shift` of the key; the key's bits
+// are tested against per-pass masks (bit_mask[b] = 1 << (shift + b)): `same`
+// collects lanes that share this lane's set bits, `diff` lanes that set one
+// of its clear bits.
+template<typename U>
+__device__ __forceinline__ uint32_t match_key_digit8(U k, const U (&bit_mask)[8]) {
+  uint32_t same = 0xffffffffu, diff = 0;
 #pragma unroll
   for(int b = 0; b < 8; ++b) {
-    const bool bit = (d >> b) & 1u;
+    const bool bit = (k & bit_mask[b]) != 0;
     const uint32_t v = __ballot_sync(0xffffffffu, bit);
-    m &= bit ? v : ~v;
+    if(bit) same &= v;
+    else diff |= v;
   }
-  return m;
+  return same & ~diff;
 }
 
 // Decoupled look-back of one digit: the sum of the counts of all predecessor
@@ -238,16 +241,19 @@ struct lookback_window_t {
           raise_error(error, err_lookback_timeout);
           return excl;
         }
+        // The predecessor has not published yet: yield issue slots to the
+        // other warps on this SM for a short while before polling again.
+        __nanosleep(128);
       }
       load();
     }
   }
 };
 
-template<typename K, typename V, int NT, int ITEMS, int WINDOW = 4, int CHAINS = 1>
+template<typename K, typename V, int NT, int ITEMS, int WINDOW = 4>
 __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const onesweep_tile_t& t, unsigned char* smem) {
-  typedef onesweep_layout<K, V, NT, ITEMS, CHAINS> L;
+  typedef onesweep_layout<K, V, NT, ITEMS> L;
   typedef typename L::U U;
   constexpr int TILE = L::tile;
   constexpr int NWARPS = L::num_warps;
@@ -284,11 +290,16 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const int rem = valid - warp_base - lane;
   U k[ITEMS];
   if(bulk) {
-    bool ok = mbar_wait_bounded(bar, 0, a.error);
+    // Only warp 0 polls the barrier; the other warps sleep at the CTA
+    // barrier below instead of spending issue slots.  The mbarrier phase
+    // completion makes the copied bytes visible to warp 0, and the CTA
+    // barrier passes that on to every thread.
+    bool ok = true;
+    if(warp == 0) ok = mbar_wait_bounded(bar, 0, a.error);
     if(__syncthreads_or(!ok)) {
       // The copy did not complete in time: wait once more (bounded) so no
       // bulk copy is still writing this CTA's shared memory, then leave.
-      mbar_wait_bounded(bar, 0, a.error);
+      if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
       return;
     }
 #pragma unroll
@@ -312,29 +323,52 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   // Warp-level stable ranking: item i of every lane forms one row; lanes
   // holding equal digits are peers.  The rank counts earlier rows and lower
   // lanes of the same row (element order), via a per-warp digit counter.
-  // Chain c covers rows [c * RPC, (c + 1) * RPC) with counters
-  // whist[warp][c][256]; one step advances every chain by one row.
-  constexpr int RPC = ITEMS / CHAINS;
   uint32_t r[ITEMS];
-  uint32_t* wh = whist + warp * CHAINS * radix_bins;
+  uint32_t* wh = whist + warp * radix_bins;
   const uint32_t lt_mask = lanemask_lt();
-#pragma unroll
-  for(int step = 0; step < RPC; ++step) {
-    uint32_t d[CHAINS], peers[CHAINS], cnt[CHAINS];
-#pragma unroll
-    for(int c = 0; c < CHAINS; ++c) {
-      d[c] = extract_digit(k[c * RPC + step], a.shift, 8);
-      peers[c] = match_digit8(d[c]);
-      cnt[c] = wh[c * radix_bins + d[c]];
-    }
+  if constexpr(L::match_in_slice) {
+    // Peers through match masks: every lane ORs its lane bit into
+    // mask[digit] and reads the word back.  The masks live in this warp's own
+    // slice of the key buffer (its keys are already in registers).  Rows
+    // alternate between two banks; the lowest peer clears its entry after the
+    // row, so a bank is clean again two rows later.
+    uint32_t* mm = (uint32_t*)(ks + warp_base);
     __syncwarp();
-#pragma unroll
-    for(int c = 0; c < CHAINS; ++c) {
-      uint32_t below = peers[c] & lt_mask;
-      if(!below) wh[c * radix_bins + d[c]] = cnt[c] + __popc(peers[c]);
-      r[c * RPC + step] = cnt[c] + __popc(below);
-    }
+    for(int j = lane; j < 2 * radix_bins; j += 32) mm[j] = 0;
     __syncwarp();
+    const uint32_t lane_bit = 1u << lane;
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      uint32_t* bank = mm + (i & 1) * radix_bins;
+      const uint32_t d = extract_digit(k[i], a.shift, 8);
+      atomicOr(&bank[d], lane_bit);
+      __syncwarp();
+      const uint32_t peers = bank[d];
+      const uint32_t cnt = wh[d];
+      __syncwarp();
+      const uint32_t below = peers & lt_mask;
+      if(!below) {
+        wh[d] = cnt + __popc(peers);
+        bank[d] = 0;
+      }
+      r[i] = cnt + __popc(below);
+    }
+  } else {
+    // Peers through one ballot per digit bit.
+    U bit_mask[8];
+#pragma unroll
+    for(int b = 0; b < 8; ++b) bit_mask[b] = (U)1 << (a.shift + b);
+#pragma unroll
+    for(int i = 0; i < ITEMS; ++i) {
+      const uint32_t d = extract_digit(k[i], a.shift, 8);
+      const uint32_t peers = match_key_digit8(k[i], bit_mask);
+      const uint32_t cnt = wh[d];
+      __syncwarp();
+      const uint32_t below = peers & lt_mask;
+      if(!below) wh[d] = cnt + __popc(peers);
+      __syncwarp();
+      r[i] = cnt + __popc(below);
+    }
   }
   __syncthreads();
 
@@ -344,7 +378,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   uint32_t tile_cnt = 0, glob_cnt = 0, valid_cnt = 0;
   if(tid < radix_bins) {
 #pragma unroll 4
-    for(int w = 0; w < NWARPS * CHAINS; ++w) {
+    for(int w = 0; w < NWARPS; ++w) {
       uint32_t c = whist[w * radix_bins + tid];
       whist[w * radix_bins + tid] = tile_cnt;
       tile_cnt += c;
@@ -362,7 +396,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   if(tid < radix_bins) {
     if(tile > 0) lbw.issue(t.lb_row + tid - radix_bins, tile);
 #pragma unroll 4
-    for(int w = 0; w < NWARPS * CHAINS; ++w) whist[w * radix_bins + tid] += tile_start;
+    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] += tile_start;
   }
   __syncthreads();
 
@@ -371,7 +405,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 #pragma unroll
   for(int i = 0; i < ITEMS; ++i) {
     uint32_t d = extract_digit(k[i], a.shift, 8);
-    r[i] += wh[(i / RPC) * radix_bins + d];
+    r[i] += wh[d];
     ks[r[i]] = k[i];
   }
   if constexpr(HAS_V) {
@@ -420,7 +454,11 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     if(j * NT < out_rem) {
       if(a.last) {
         K key = radix_key<K>::from_bits(u[j]);
-        memcpy(&keys_out[dst[j]], &key, sizeof(K));
+        // Convert in registers and store one word (a memcpy straight to
+        // global memory may be split into narrow stores).
+        U out;
+        memcpy(&out, &key, sizeof(U));
+        keys_out[dst[j]] = out;
       } else {
         keys_out[dst[j]] = u[j];
       }
@@ -433,13 +471,12 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
 }
 
-template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int WINDOW = 4,
-  int CHAINS = 1>
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int WINDOW = 4>
 __global__ void __launch_bounds__(NT, MIN_BLOCKS)
 onesweep_pass(onesweep_args<K, V> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int TILE = NT * ITEMS;
-  const int tile = onesweep_begin<K, V, NT, ITEMS, CHAINS>(a.tile_counter, smem);
+  const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
   onesweep_tile_t t;
   t.base = (int64_t)tile * TILE;
   t.valid = (int)min((int64_t)TILE, a.count - t.base);
@@ -447,7 +484,7 @@ onesweep_pass(onesweep_args<K, V> a) {
   t.lb_row = a.lookback + (int64_t)tile * radix_bins;
   t.hist = a.hist;
   t.out_base = 0;
-  onesweep_tile<K, V, NT, ITEMS, WINDOW, CHAINS>(a, t, smem);
+  onesweep_tile<K, V, NT, ITEMS, WINDOW>(a, t, smem);
 }
 
 }  // namespace device

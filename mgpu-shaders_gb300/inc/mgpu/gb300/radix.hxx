@@ -8,8 +8,8 @@
 // examples/vk_radix/vk_radix.cxx:56).  Key-value sorting is an addition.
 //
 // Launch sequence per sort: one memset of the small header (histograms and
-// tile counters), radix_histogram (all digit places, also clears the
-// look-back words), then one onesweep_pass per digit, ping-ponging between
+// tile counters), radix_histogram (all digit places), then per digit a
+// memset of that pass's look-back words and one onesweep_pass, ping-ponging between
 // `keys`/`vals` and the aux copies.  The pass count is even for 4- and 8-byte
 // keys, so the result lands in the caller's buffers.  No host
 // synchronisation: the sequence is stream-ordered and graph-capturable.
@@ -24,7 +24,7 @@ namespace gb300 {
 
 // Default tile shapes per key width (threads, keys per thread, CTAs per SM).
 template<int key_bytes> struct radix_tuning;
-template<> struct radix_tuning<4> { enum { nt = 512, vt = 16, min_blocks = 2 }; };
+template<> struct radix_tuning<4> { enum { nt = 256, vt = 20, min_blocks = 3 }; };
 template<> struct radix_tuning<8> { enum { nt = 256, vt = 12, min_blocks = 3 }; };
 
 // Largest count the 30-bit look-back status word can carry.
@@ -65,7 +65,6 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
   size_t header_off = lay.add(sizeof(uint32_t) * (passes * radix_bins + passes));
   size_t header_bytes = lay.total;
   size_t lookback_off = lay.add(sizeof(uint32_t) * radix_bins * passes * num_tiles);
-  size_t lookback_bytes = lay.total - lookback_off;
   size_t keys_off = lay.add(sizeof(K) * count);
   size_t vals_off = has_values ? lay.add(sizeof(V) * count) : 0;
   (void)header_off;
@@ -92,7 +91,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     int vec = aligned16_host(keys);
     st = ctx.launch("radix_histogram", [&] {
       radix_histogram<K, hnt, passes><<<grid, hnt, 0, ctx.stream>>>(keys, count, hist,
-        (uint4*)lookback, (int64_t)(lookback_bytes / 16), vec);
+        (uint4*)lookback, 0, vec);
     });
     if(st) return st;
   }
@@ -117,6 +116,10 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     a.first = p == 0;
     a.last = p == passes - 1;
     a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));
+    // Clear this pass's look-back words right before it runs, so they are
+    // still in L2 when tiles poll them.
+    if(ctx.check(cudaMemsetAsync(a.lookback, 0, sizeof(uint32_t) * num_tiles * radix_bins,
+      ctx.stream))) return MGPU_ERR_CUDA;
     st = ctx.launch("onesweep_pass", [&] {
       kernel<<<(unsigned)num_tiles, nt, L::bytes, ctx.stream>>>(a);
     });
