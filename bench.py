@@ -122,11 +122,11 @@ def dist_info():
     return rank, world, local
 
 
-def cpu_baseline(threads, sample=CPU_SAMPLE, min_seconds=10.0, max_reps=8):
+def cpu_baseline(threads, sample=CPU_SAMPLE, min_seconds=10.0, max_reps=8, dist="uniform"):
     """The host oracle's parallel stable radix-order sort on `sample` keys,
     repeated until about min_seconds of CPU work; Mkeys/s (median)."""
     from oracle import oracle
-    k0, v0 = make_input(sample)
+    k0, v0 = make_input(sample, dist)
     rates = []
     t_total = 0.0
     while len(rates) < max_reps and (t_total < min_seconds or len(rates) < 3):
@@ -146,7 +146,7 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     from oracle import oracle
-    k0, v0 = make_input(CPU_SAMPLE)
+    k0, v0 = make_input(CPU_SAMPLE, args.dist)
     for _ in range(args.warmup):
         k, v = k0.copy(), v0.copy()
         oracle.sort_parallel_inplace(k, v, "radix", threads)
@@ -163,7 +163,7 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": config(),
+        "config": config(args.dist),
         "cpu_baseline": {"value": value, "unit": "Mkeys/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "Mkeys/s", "h2d_bytes_per_step": 0,
@@ -171,6 +171,590 @@ def run_reference(args):
         "note": "reference shaders need Circle + Vulkan (unavailable on this box); timed: the "
                 "host oracle's std::thread stable sort by radix bits",
     }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# Further workloads (--workload NAME): one JSON line each, same timing rules
+# (W >= 3 warm-up steps, CUDA events on the launching stream, inputs larger
+# than L2 or restored by a device copy outside the step's events).
+
+def _peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path)).get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def _timed(ctx, run, restore, steps, warmup, device):
+    """Runs warm-up then `steps` timed steps; returns (per-step ms, launches,
+    clocks)."""
+    import torch
+    for w in range(warmup):
+        restore(w)
+        run(w)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    clocks = ClockSampler(device)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    launches = 0
+    for i in range(steps):
+        restore(i)
+        ev[i][0].record(stream)
+        l0 = ctx.launch_count
+        run(i)
+        launches += ctx.launch_count - l0
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ctx.synchronize()
+    return [a.elapsed_time(b) for a, b in ev], launches, clk
+
+
+def _roofline(ctx, run, restore, reps, bytes_per_launch):
+    """Per-kernel event times of `reps` profiled steps; the roofline entry of
+    the kernel with the largest share."""
+    ctx.synchronize()
+    for i in range(reps):
+        restore(i)
+        ctx.profile(True)
+        run(i)
+        ctx.profile(False)
+    prof = ctx.profile_read()
+    top = max(prof, key=lambda k: prof[k][1])
+    launches, total = prof[top]
+    launch_ms = total / max(1, launches)
+    b = bytes_per_launch.get(top)
+    achieved = b / (launch_ms * 1e-3) / 1e9 if b and launch_ms else None
+    peak, src = _peak()
+    roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "traffic": None,
+            "peak_source": src, "launch_ms": launch_ms, "bytes_per_launch": b}
+    return roof, {k: v[1] / reps for k, v in prof.items()}
+
+
+def _line(metric, unit, units, alg_bytes, ms, steps, warmup, launches, clk, roof, kernels,
+          cfg, dtype, checks, higher=True, extra=None):
+    mean = sum(ms) / len(ms)
+    line = {"workload": cfg["workload"], "metric": metric,
+            "value": units / (mean * 1e-3) / 1e6 if higher else mean, "unit": unit,
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": mean,
+            "ms_median": statistics.median(ms), "higher_is_better": higher, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": cfg,
+            "gpu_launches": launches,
+            "step_gbs": alg_bytes / (mean * 1e-3) / 1e9,
+            "step_frac_of_peak": alg_bytes / (mean * 1e-3) / 1e9 / _peak()[0],
+            "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk, "checks": checks}
+    if extra:
+        line.update(extra)
+    return line
+
+
+def _radix_keys(rng, n, kind):
+    if kind == "u64":
+        return rng.integers(0, 2 ** 63, n, dtype=np.uint64) * 2 + \
+            rng.integers(0, 2, n, dtype=np.uint64)
+    if kind == "f32bits":
+        raw = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+        # Non-finite patterns (exponent all ones) get the exponent cleared.
+        bad = (raw & 0x7F800000) == 0x7F800000
+        raw[bad] &= np.uint32(0x807FFFFF)
+        return raw.view(np.float32)
+    if kind == "f32normal":
+        return rng.standard_normal(n).astype(np.float32)
+    raise ValueError(kind)
+
+
+def wl_radix_wide(args, mg, torch, kind):
+    """2^27 u64 keys (200 B/key) or f32 keys (68 B/key), int32 values = index."""
+    n = args.n if args.n != N_KEYS else 1 << 27
+    rng = np.random.default_rng(SEED + (6 if kind == "u64" else 7))
+    keys = _radix_keys(rng, n, kind)
+    vals = np.arange(n, dtype=np.int32)
+    kb = keys.dtype.itemsize
+    ctx = mg.Context(0)
+    pk, pv = mg.DeviceArray.from_numpy(keys), mg.DeviceArray.from_numpy(vals)
+    work = [(mg.DeviceArray(n, keys.dtype), mg.DeviceArray(n, np.int32)) for _ in range(2)]
+    aux_b = ctx.radix_sort_aux_size(keys.dtype, np.int32, n)
+    aux_t = torch.empty(aux_b, dtype=torch.uint8, device="cuda")
+    aux = (aux_t.data_ptr(), aux_b)
+
+    def restore(i):
+        work[i % 2][0].copy_from(pk)
+        work[i % 2][1].copy_from(pv)
+
+    def run(i):
+        ctx.radix_sort(work[i % 2][0], work[i % 2][1], aux=aux)
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
+    gk, gv = work[(steps - 1) % 2][0].numpy(), work[(steps - 1) % 2][1].numpy()
+    bits = gk.view(np.uint32) if kb == 4 else gk
+    if kind != "u64":
+        # Radix order of floats: sign-flipped bit patterns ascend.
+        b = gk.view(np.uint32)
+        bits = np.where(b >> 31 == 1, ~b, b | np.uint32(0x80000000))
+    checks = {"sorted_by_radix_bits": bool(np.all(bits[1:] >= bits[:-1])),
+              "values_permute_keys": bool(np.array_equal(keys[gv].view(np.uint8),
+                                                         gk.view(np.uint8)))}
+    passes = kb
+    per_launch = {"onesweep_pass": 2 * (kb + 4) * n}
+    roof, kernels = _roofline(ctx, run, restore, 3, per_launch)
+    alg = (passes * 2 * (kb + 4) + kb) * n
+    cfg = {"workload": "radix_sort_kv %s keys + i32 values, %d keys%s" % (
+        "u64" if kind == "u64" else "f32", n,
+        {"u64": ", uniform 64-bit", "f32bits": ", uniform finite f32 bit patterns",
+         "f32normal": ", N(0,1) f32"}[kind]),
+        "count": n, "alg_bytes_per_key": alg // n, "digit_bits": 8,
+        "l2": "inputs larger than L2, restored by a device copy outside the step's events"}
+    return _line("Mkeys/s", "Mkeys/s", n, alg, ms, steps, warmup, launches, clk, roof, kernels,
+                 cfg, "u64" if kind == "u64" else "f32", checks)
+
+
+def wl_mergesort(args, mg, torch):
+    """2^20 u32 keys + int32 index values, std::less; 192 B/key (the
+    reference's pass structure at nt=128, vt=7)."""
+    n = args.n if args.n != N_KEYS else 1 << 20
+    k, v = make_input(n, seed=SEED + 1)
+    ctx = mg.Context(0)
+    pk, pv = mg.DeviceArray.from_numpy(k), mg.DeviceArray.from_numpy(v.view(np.int32))
+    wk, wv = mg.DeviceArray(n, np.uint32), mg.DeviceArray(n, np.int32)
+
+    def restore(i):
+        wk.copy_from(pk)
+        wv.copy_from(pv)
+
+    def run(i):
+        ctx.mergesort(wk, wv)
+
+    steps, warmup = max(args.steps, 20), max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
+    gk, gv = wk.numpy(), wv.numpy()
+    order = np.argsort(k, kind="stable")
+    checks = {"equals_stable_sort": bool(np.array_equal(gk, k[order]) and
+                                         np.array_equal(gv, order.astype(np.int32)))}
+    per_launch = {"mergesort_pass": 16 * n, "blocksort": 16 * n}
+    roof, kernels = _roofline(ctx, run, restore, 3, per_launch)
+    passes = 1 + int(np.ceil(np.log2(np.ceil(n / 896))))
+    alg = passes * 16 * n
+    cfg = {"workload": "mergesort_kv u32 keys + i32 index values, %d keys, std::less" % n,
+           "count": n, "alg_bytes_per_key": alg // n,
+           "l2": "8 MiB working set is L2-resident; restored by a device copy outside the "
+                 "step's events"}
+    return _line("Mkeys/s", "Mkeys/s", n, alg, ms, steps, warmup, launches, clk, roof, kernels,
+                 cfg, "u32", checks)
+
+
+def wl_merge(args, mg, torch):
+    """A, B: 2^26 int32 each from U[0, 2^24), sorted; int32 values; 16 B per
+    output element."""
+    na = args.n if args.n != N_KEYS else 1 << 26
+    rng = np.random.default_rng(SEED + 2)
+    a = np.sort(rng.integers(0, 1 << 24, na).astype(np.int32))
+    b = np.sort(rng.integers(0, 1 << 24, na).astype(np.int32))
+    av = np.arange(na, dtype=np.int32)
+    bv = np.arange(na, dtype=np.int32) + na
+    ctx = mg.Context(0)
+    da, db = mg.DeviceArray.from_numpy(a), mg.DeviceArray.from_numpy(b)
+    dav, dbv = mg.DeviceArray.from_numpy(av), mg.DeviceArray.from_numpy(bv)
+    dc, dcv = mg.DeviceArray(2 * na, np.int32), mg.DeviceArray(2 * na, np.int32)
+
+    def run(i):
+        ctx.merge(da, dav, db, dbv, dc, dcv)
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, lambda i: None, steps, warmup, 0)
+    gk, gv = dc.numpy(), dcv.numpy()
+    ab = np.concatenate([a, b])
+    checks = {"sorted": bool(np.all(gk[1:] >= gk[:-1])),
+              "values_permute_keys": bool(np.array_equal(ab[gv], gk)),
+              "ties_take_a_first": bool(np.all((gk[1:] != gk[:-1]) | (gv[1:] > gv[:-1]) |
+                                               ((gv[1:] >= na) & (gv[:-1] < na))))}
+    out = 2 * na
+    roof, kernels = _roofline(ctx, run, lambda i: None, 3, {"merge": 16 * out})
+    cfg = {"workload": "merge_kv int32 keys + int32 values, A = B = %d from U[0,2^24)" % na,
+           "count": out, "alg_bytes_per_output": 16, "l2": "inputs larger than L2"}
+    return _line("Mkeys/s (merged outputs)", "Mkeys/s", out, 16 * out, ms, steps, warmup,
+                 launches, clk, roof, kernels, cfg, "int32", checks)
+
+
+def wl_scan(args, mg, torch, kind):
+    """int32 U[0,100) 2^28 elements, exclusive and inclusive plus; or f32
+    N(0,1) 2^26 elements, inclusive plus.  8 B/element."""
+    rng = np.random.default_rng(SEED + (3 if kind == "i32" else 4))
+    if kind == "i32":
+        n = args.n if args.n != N_KEYS else 1 << 28
+        x = rng.integers(0, 100, n).astype(np.int32)
+    else:
+        n = args.n if args.n != N_KEYS else 1 << 26
+        x = rng.standard_normal(n).astype(np.float32)
+    ctx = mg.Context(0)
+    dx, dy = mg.DeviceArray.from_numpy(x), mg.DeviceArray(n, x.dtype)
+    steps, warmup = args.steps, max(3, args.warmup)
+    results = {}
+    for st in (["exc", "inc"] if kind == "i32" else ["inc"]):
+        def run(i, st=st):
+            ctx.scan(dx, dy, scan_type=st)
+        ms, launches, clk = _timed(ctx, run, lambda i: None, steps, warmup, 0)
+        y = dy.numpy()
+        if kind == "i32":
+            ref = np.cumsum(x, dtype=np.int64).astype(np.int32)
+            if st == "exc":
+                ref = np.concatenate([[0], ref[:-1]]).astype(np.int32)
+            ok = bool(np.array_equal(y, ref))
+        else:
+            ref = np.cumsum(x.astype(np.float64))
+            mag = np.cumsum(np.abs(x.astype(np.float64)))
+            # fp32 sums in tile order: error bounded by a few ulps of the
+            # running sum of magnitudes.
+            ok = bool(np.all(np.abs(y - ref) <= 2e-5 * mag + 1e-6))
+        roof, kernels = _roofline(ctx, run, lambda i: None, 3,
+                                  {"scan_exc": 8 * n, "scan_inc": 8 * n})
+        results[st] = (ms, launches, clk, roof, kernels, ok)
+    st0 = "exc" if kind == "i32" else "inc"
+    ms, launches, clk, roof, kernels, ok = results[st0]
+    extra = {}
+    if kind == "i32":
+        m2 = results["inc"][0]
+        extra["inclusive"] = {"value": n / (sum(m2) / len(m2) * 1e-3) / 1e6,
+                              "ms_per_step": sum(m2) / len(m2), "roofline": results["inc"][3],
+                              "check": results["inc"][5]}
+    cfg = {"workload": ("scan int32 U[0,100), %d elements, exclusive plus" % n) if kind == "i32"
+           else "scan f32 N(0,1), %d elements, inclusive plus" % n,
+           "count": n, "alg_bytes_per_elem": 8, "l2": "inputs larger than L2"}
+    return _line("Melems/s", "Melems/s", n, 8 * n, ms, steps, warmup, launches, clk, roof,
+                 kernels, cfg, "int32" if kind == "i32" else "f32",
+                 {"matches_host_scan": ok}, extra=extra)
+
+
+def _lognormal_offsets(rng, num_segments, median=256, sigma=2.0, hi=1 << 20):
+    lens = np.clip(np.exp(rng.normal(np.log(median), sigma, num_segments)).round(), 1, hi)
+    off = np.zeros(num_segments + 1, np.int64)
+    np.cumsum(lens.astype(np.int64), out=off[1:])
+    return off
+
+
+def wl_segsort(args, mg, torch):
+    """100,000 segments, lengths lognormal(ln 256, 2) clipped to [1, 2^20],
+    u32 keys + u32 index values; 16 B/key.  Compared with the same segments
+    sorted by per-segment plain radix_sort calls on the same GPU, both as a
+    host loop and captured into one CUDA graph."""
+    rng = np.random.default_rng(SEED + 8)
+    off = _lognormal_offsets(rng, 100_000)
+    n = int(off[-1])
+    keys = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    ctx = mg.Context(0)
+    pk, pv = mg.DeviceArray.from_numpy(keys), mg.DeviceArray.from_numpy(vals)
+    doff = mg.DeviceArray.from_numpy(off)
+    wk, wv = mg.DeviceArray(n, np.uint32), mg.DeviceArray(n, np.uint32)
+
+    def restore(i):
+        wk.copy_from(pk)
+        wv.copy_from(pv)
+
+    def run(i):
+        ctx.segmented_sort(wk, wv, doff)
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
+    gk, gv = wk.numpy(), wv.numpy()
+    seg_id = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    order = np.lexsort((keys, seg_id))
+    checks = {"equals_per_segment_stable_sort": bool(np.array_equal(gk, keys[order]) and
+                                                     np.array_equal(gv, order.astype(np.uint32)))}
+    # Segments of up to one 5120-key tile sort inside seg_small_sort; larger
+    # ones go through seg_onesweep_pass, one launch per digit.
+    seg_lens = np.diff(off)
+    small_keys = int(seg_lens[seg_lens <= 5120].sum())
+    roof, kernels = _roofline(ctx, run, restore, 3,
+                              {"seg_small_sort": 16 * small_keys,
+                               "seg_onesweep_pass": 16 * (n - small_keys)})
+    # Per-segment plain calls (the C ABI's radix sort on each segment).
+    lib = mg.lib()
+    pctx = mg.Context(0, use_torch_stream=False)
+    pctx.cache_reserve(pctx.radix_sort_aux_size(np.uint32, np.uint32, int(np.diff(off).max())))
+    lens = np.diff(off)
+
+    def plain_loop():
+        kp, vp, h = wk.ptr, wv.ptr, pctx.handle
+        for s, ln in zip(off[:-1].tolist(), lens.tolist()):
+            rc = lib.mgpu_radix_sort(h, 1, kp + 4 * s, 4, vp + 4 * s, ln, None, None)
+            if rc:
+                pctx._check(rc)
+
+    def plain_restore():
+        pctx._check(lib.mgpu_memcpy(pctx.handle, wk.ptr, pk.ptr, 4 * n))
+        pctx._check(lib.mgpu_memcpy(pctx.handle, wv.ptr, pv.ptr, 4 * n))
+
+    torch.cuda.synchronize()
+    plain_restore()
+    plain_loop()                    # warm-up (grows nothing: the cache is reserved)
+    pctx.synchronize()
+    plain_restore()
+    pctx.synchronize()
+    t = time.perf_counter()
+    plain_loop()
+    pctx.synchronize()
+    loop_ms = 1e3 * (time.perf_counter() - t)
+    loop_ok = bool(np.array_equal(wk.numpy(), keys[order]))
+    pctx.graph_begin()
+    plain_loop()
+    g = pctx.graph_end()
+    plain_restore()
+    g.launch()                      # warm-up launch of the graph
+    pctx.synchronize()
+    graph_ms = []
+    for _ in range(3):
+        plain_restore()
+        pctx.synchronize()
+        t = time.perf_counter()
+        g.launch()
+        pctx.synchronize()
+        graph_ms.append(1e3 * (time.perf_counter() - t))
+    graph_ok = bool(np.array_equal(wk.numpy(), keys[order]))
+    g.close()
+    mean = sum(ms) / len(ms)
+    cfg = {"workload": "segmented_sort u32 keys + u32 values, 100000 lognormal(ln 256, 2) "
+                       "segments clipped to [1, 2^20], %d keys" % n,
+           "count": n, "segments": 100_000, "alg_bytes_per_key": 16,
+           "l2": "inputs larger than L2, restored by a device copy outside the step's events"}
+    extra = {"plain_calls": {
+        "host_loop_ms": loop_ms, "graph_ms": statistics.median(graph_ms),
+        "speedup_vs_host_loop": loop_ms / mean,
+        "speedup_vs_graph": statistics.median(graph_ms) / mean,
+        "checks": {"host_loop": loop_ok, "graph": graph_ok}}}
+    return _line("Mkeys/s", "Mkeys/s", n, 16 * n, ms, steps, warmup, launches, clk, roof,
+                 kernels, cfg, "u32", checks, extra=extra)
+
+
+def wl_segscan(args, mg, torch):
+    """The segmented-sort segments over int32 U[0,100) values, inclusive
+    plus; 8 B/element."""
+    rng = np.random.default_rng(SEED + 8)
+    off = _lognormal_offsets(rng, 100_000)
+    n = int(off[-1])
+    x = rng.integers(0, 100, n).astype(np.int32)
+    ctx = mg.Context(0)
+    dx, dy = mg.DeviceArray.from_numpy(x), mg.DeviceArray(n, np.int32)
+    doff = mg.DeviceArray.from_numpy(off)
+
+    def run(i):
+        ctx.segmented_scan(dx, dy, doff, scan_type="inc")
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, lambda i: None, steps, warmup, 0)
+    y = dy.numpy()
+    c = np.cumsum(x, dtype=np.int64)
+    start = np.repeat(np.concatenate([[0], c])[off[:-1]], np.diff(off))
+    ok = bool(np.array_equal(y, (c - start).astype(np.int32)))
+    roof, kernels = _roofline(ctx, run, lambda i: None, 3, {"seg_scan": 8 * n})
+    cfg = {"workload": "segmented_scan int32 U[0,100), inclusive plus, the 100000 "
+                       "lognormal segments, %d elements" % n,
+           "count": n, "segments": 100_000, "alg_bytes_per_elem": 8,
+           "l2": "inputs larger than L2"}
+    return _line("Melems/s", "Melems/s", n, 8 * n, ms, steps, warmup, launches, clk, roof,
+                 kernels, cfg, "int32", {"matches_host_segmented_scan": ok})
+
+
+def wl_serving(args, mg, torch):
+    """Serving: Poisson arrivals of sort / merge / scan requests, sizes
+    log-uniform in [2^10, 2^26] elements, key types u32 / u64 / f32 at
+    50/25/25 %, under a 64 GiB budget.  Saturation is the throughput with all
+    requests queued at once; arrivals then run at 0.5x and 0.9x of it, and
+    the same arrival traces are served by serial plain calls (one request at a
+    time: copy in, primitive, copy out, synchronise)."""
+    rng = np.random.default_rng(SEED + 9)
+    max_log2 = args.serve_max_log2
+    pool = []
+    for i in range(args.serve_pool):
+        op = ("sort", "merge", "scan")[i % 3]
+        kt = (np.uint32, np.uint32, np.uint64, np.float32)[rng.integers(0, 4)]
+        n = int(2 ** rng.uniform(10, max_log2))
+        kt = np.dtype(kt)
+        if kt.kind == "f":
+            gen = lambda m: rng.standard_normal(m).astype(np.float32)   # noqa: E731
+        else:
+            gen = lambda m: _radix_keys(rng, m, "u64").astype(kt)        # noqa: E731
+
+        def pin(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).pin_memory()
+
+        def empty(nbytes):
+            return torch.empty(max(1, nbytes), dtype=torch.uint8).pin_memory()
+
+        r = mg.Request(op=mg.REQ_OPS[op], key_type=mg.DTYPES[kt], count=n)
+        if op == "sort":
+            held = [pin(gen(n)), pin(np.arange(n, dtype=np.uint32)),
+                    empty(n * kt.itemsize), empty(4 * n)]
+            r.val_bytes = 4
+            r.keys, r.vals, r.out_keys, r.out_vals = [h.data_ptr() for h in held]
+        elif op == "merge":
+            na = n // 2
+            nb = n - na
+            r.count, r.count_b, r.val_bytes = na, nb, 4
+            held = [pin(np.sort(gen(na))), pin(np.arange(na, dtype=np.uint32)),
+                    pin(np.sort(gen(nb))), pin(np.arange(nb, dtype=np.uint32) + na),
+                    empty(n * kt.itemsize), empty(4 * n)]
+            r.keys, r.vals, r.keys_b, r.vals_b, r.out_keys, r.out_vals = \
+                [h.data_ptr() for h in held]
+        else:
+            held = [pin(gen(n)), empty(n * kt.itemsize)]
+            r.scan_type = 1 if kt.kind == "f" else 0
+            r.keys, r.out_keys = held[0].data_ptr(), held[1].data_ptr()
+        pool.append((op, kt, n, r, held))
+    elems = np.array([p[2] for p in pool], dtype=np.float64)
+
+    srv = mg.Server(0, budget_bytes=args.serve_budget_gb << 30, num_slots=args.serve_slots)
+    for p in pool:                                      # warm-up: each request once
+        srv.submit(p[3], p[4])
+    srv.drain()
+
+    # Saturation: every request queued at once.
+    order = np.concatenate([rng.permutation(len(pool)) for _ in range(args.serve_reps)])
+    srv.reset_stats()
+    t = time.perf_counter()
+    ids = [srv.submit(pool[j][3], pool[j][4]) for j in order]
+    for rid in ids:
+        srv.wait(rid)
+    sat_s = time.perf_counter() - t
+    sat = srv.stats()
+    sat_rps = len(order) / sat_s
+    sat_line = {"requests": len(order), "seconds": sat_s, "requests_per_s": sat_rps,
+                "mkeys_per_s": elems[order].sum() / sat_s / 1e6, "p50_ms": sat["p50_ms"],
+                "p99_ms": sat["p99_ms"], "peak_bytes": sat["peak_bytes"]}
+
+    # Serial plain calls: one context, device buffers sized for the largest request.
+    ctx = mg.Context(0, use_torch_stream=False)
+    lib = mg.lib()
+    big = max(p[2] for p in pool) * 8
+    dev = [mg.DeviceArray(big, np.uint8) for _ in range(6)]
+
+    def view(i, count, dt):
+        return mg.DeviceArray(count, dt, tensor=dev[i].tensor)
+
+    def cp(dst, src, nbytes):
+        if nbytes:
+            ctx._check(lib.mgpu_memcpy(ctx.handle, dst, src, nbytes))
+
+    def serve_plain(p):
+        op, kt, n, r, held = p
+        if op == "sort":
+            cp(dev[0].ptr, r.keys, n * kt.itemsize)
+            cp(dev[1].ptr, r.vals, 4 * n)
+            ctx.radix_sort(view(0, n, kt), view(1, n, np.uint32))
+            cp(r.out_keys, dev[0].ptr, n * kt.itemsize)
+            cp(r.out_vals, dev[1].ptr, 4 * n)
+        elif op == "merge":
+            na, nb = r.count, r.count_b
+            cp(dev[0].ptr, r.keys, na * kt.itemsize)
+            cp(dev[1].ptr, r.vals, 4 * na)
+            cp(dev[2].ptr, r.keys_b, nb * kt.itemsize)
+            cp(dev[3].ptr, r.vals_b, 4 * nb)
+            ctx.merge(view(0, na, kt), view(1, na, np.uint32), view(2, nb, kt),
+                      view(3, nb, np.uint32), view(4, n, kt), view(5, n, np.uint32))
+            cp(r.out_keys, dev[4].ptr, n * kt.itemsize)
+            cp(r.out_vals, dev[5].ptr, 4 * n)
+        else:
+            cp(dev[0].ptr, r.keys, n * kt.itemsize)
+            ctx.scan(view(0, n, kt), view(1, n, kt), scan_type="inc" if r.scan_type else "exc")
+            cp(r.out_keys, dev[1].ptr, n * kt.itemsize)
+        ctx.synchronize()
+
+    for p in pool:                                      # warm-up (grows the aux cache)
+        serve_plain(p)
+    t = time.perf_counter()
+    for j in order:
+        serve_plain(pool[j])
+    serial_s = time.perf_counter() - t
+    serial_sat = {"requests_per_s": len(order) / serial_s,
+                  "mkeys_per_s": elems[order].sum() / serial_s / 1e6}
+
+    def pct(x, q):
+        x = sorted(x)
+        return x[min(len(x) - 1, int(round(q * (len(x) - 1))))]
+
+    loads = []
+    for load in (0.5, 0.9):
+        lam = load * sat_rps
+        num = int(min(max(2 * len(pool), lam * args.serve_seconds), 20000))
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, num))
+        picks = rng.integers(0, len(pool), num)
+        # Served by the server.
+        srv.reset_stats()
+        ids = []
+        t0 = time.perf_counter()
+        for a, j in zip(arrivals, picks):
+            while time.perf_counter() - t0 < a:
+                left = a - (time.perf_counter() - t0)
+                if left > 2e-3:
+                    time.sleep(left - 1e-3)
+            ids.append(srv.submit(pool[j][3], pool[j][4]))
+        for rid in ids:
+            srv.wait(rid)
+        span = time.perf_counter() - t0
+        st = srv.stats()
+        # Served by serial plain calls on the same arrival trace.
+        lat = []
+        t0 = time.perf_counter()
+        for a, j in zip(arrivals, picks):
+            now = time.perf_counter() - t0
+            if now < a:
+                time.sleep(a - now)
+            serve_plain(pool[j])
+            lat.append(1e3 * (time.perf_counter() - t0 - a))
+        serial_span = time.perf_counter() - t0
+        loads.append({
+            "load": load, "lambda_per_s": lam, "requests": num,
+            "server": {"requests_per_s": num / span, "mkeys_per_s": elems[picks].sum() / span / 1e6,
+                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                       "max_ms": st["max_ms"], "failed": st["failed"],
+                       "peak_bytes": st["peak_bytes"]},
+            "serial_plain_calls": {"requests_per_s": num / serial_span,
+                                   "mkeys_per_s": elems[picks].sum() / serial_span / 1e6,
+                                   "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99)}})
+    srv.close()
+    hi = loads[-1]
+    cfg = {"workload": "serving: Poisson arrivals of sort/merge/scan requests, sizes "
+                       "log-uniform 2^10..2^%d, u32/u64/f32 keys 50/25/25" % max_log2,
+           "pool_requests": len(pool), "slots": args.serve_slots,
+           "budget_bytes": args.serve_budget_gb << 30,
+           "sort": "keys + u32 values", "merge": "two sorted halves + u32 values",
+           "scan": "exclusive plus (integers), inclusive plus (f32)",
+           "l2": "requests stream from pinned host memory (copies inside each request)"}
+    return {"workload": cfg["workload"], "metric": "requests/s at 0.9x saturation",
+            "value": hi["server"]["requests_per_s"], "unit": "requests/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32/u64/f32", "data": "synthetic", "config": cfg,
+            "saturation": sat_line, "serial_saturation": serial_sat, "loads": loads,
+            "p50_ms": hi["server"]["p50_ms"], "p99_ms": hi["server"]["p99_ms"]}
+
+
+WORKLOADS = {
+    "radix_u64": lambda a, m, t: wl_radix_wide(a, m, t, "u64"),
+    "radix_f32": lambda a, m, t: wl_radix_wide(a, m, t, "f32bits"),
+    "radix_f32_normal": lambda a, m, t: wl_radix_wide(a, m, t, "f32normal"),
+    "mergesort": wl_mergesort,
+    "merge": wl_merge,
+    "scan_i32": lambda a, m, t: wl_scan(a, m, t, "i32"),
+    "scan_f32": lambda a, m, t: wl_scan(a, m, t, "f32"),
+    "segsort": wl_segsort,
+    "segscan": wl_segscan,
+    "serving": wl_serving,
+}
+
+
+def run_workload(args):
+    import torch
+    import mgpu_gb300 as mg
+    torch.cuda.set_device(0)
+    line = WORKLOADS[args.workload](args, mg, torch)
     print(json.dumps(line))
     return 0
 
@@ -183,9 +767,20 @@ def main():
     ap.add_argument("--impl", default="mgpu", choices=["mgpu", "reference"])
     ap.add_argument("--n", type=int, default=N_KEYS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dist", default="uniform", choices=["uniform", "and2", "distinct256"],
+                    help="key entropy of the headline radix workload")
+    ap.add_argument("--workload", default="radix", choices=["radix"] + sorted(WORKLOADS))
+    ap.add_argument("--serve-pool", type=int, default=24)
+    ap.add_argument("--serve-reps", type=int, default=3)
+    ap.add_argument("--serve-max-log2", type=int, default=26)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-budget-gb", type=int, default=64)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "radix":
+        return run_workload(args)
 
     import torch
     import mgpu_gb300 as mg
@@ -201,7 +796,7 @@ def main():
     n = args.n
     steps, warmup = args.steps, max(3, args.warmup)
     ctx = mg.Context(local)
-    keys_h, vals_h = make_input(n, seed=SEED + rank)
+    keys_h, vals_h = make_input(n, dist=args.dist, seed=SEED + rank)
 
     # Each step sorts an unsorted 2 GiB copy (> L2), restored from the pristine
     # input by a device copy that lies outside the step's event pair.
@@ -307,7 +902,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "Mkeys/s", "n_gpus": world, "steps": steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config(),
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config(args.dist),
         "gpu_launches": launches,
         "hbm_gbs_at_68B_per_key": ALG_BYTES_PER_KEY * n / (ms * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "kernel": "onesweep_pass", "achieved": achieved,
@@ -324,7 +919,7 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, reps = cpu_baseline(threads)
+        v, reps = cpu_baseline(threads, dist=args.dist)
         line["cpu_baseline"] = {
             "value": v, "unit": "Mkeys/s", "cores": threads, "kind": "port",
             "sample": "%d-key sample of the same generator, %d runs (median), host oracle "

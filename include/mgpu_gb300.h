@@ -240,6 +240,67 @@ MGPU_API mgpu_status_t mgpu_graph_destroy(mgpu_graph_t* graph);
 /* Grows the context's aux cache to at least `bytes` (stream-ordered). */
 MGPU_API mgpu_status_t mgpu_cache_reserve(mgpu_context_t* ctx, size_t bytes);
 
+/* ---- serving: continuous batching of sort / merge / scan requests (no
+ * reference counterpart).  A scheduler thread admits queued requests, in
+ * arrival order, whenever a stream slot is free and the request's device
+ * footprint (inputs, outputs and aux) fits in the remaining HBM budget;
+ * admitted requests copy their host inputs into device buffers drawn from a
+ * stream-ordered pool that stays resident, run the primitive on the slot's
+ * stream, copy the results back and release their memory, so requests that
+ * arrive while others run overlap with them.  Host buffers must stay valid
+ * until the request completes (pinned memory gives asynchronous copies). */
+typedef enum mgpu_request_op_t {
+  MGPU_REQ_SORT = 0,   /* radix sort of keys (+ values), in place on device */
+  MGPU_REQ_MERGE = 1,  /* merge of sorted A and B (+ values) */
+  MGPU_REQ_SCAN = 2    /* scan of `count` elements */
+} mgpu_request_op_t;
+
+typedef struct mgpu_request_t {
+  int op;                  /* mgpu_request_op_t */
+  mgpu_dtype_t key_type;   /* keys (sort, merge) or elements (scan) */
+  int val_bytes;           /* values of sort / merge: 0, 4 or 8 */
+  int64_t count;           /* sort / scan elements; merge: A count */
+  int64_t count_b;         /* merge: B count */
+  const void* keys;        /* host: sort keys, scan input, merge A keys */
+  const void* vals;        /* host: sort values, merge A values */
+  const void* keys_b;      /* host: merge B keys */
+  const void* vals_b;      /* host: merge B values */
+  void* out_keys;          /* host: sorted keys, merged keys, scan output */
+  void* out_vals;          /* host: sorted / merged values */
+  int scan_type;           /* scan: mgpu_scan_type_t */
+  int op_arg;              /* scan: mgpu_op_t; merge: mgpu_comp_t */
+} mgpu_request_t;
+
+typedef struct mgpu_server_stats_t {
+  int64_t submitted, completed, failed;
+  int64_t elements;        /* sum of request element counts completed */
+  double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> completion */
+  size_t peak_bytes;       /* largest admitted footprint total */
+} mgpu_server_stats_t;
+
+typedef struct mgpu_server mgpu_server_t;
+/* `budget_bytes` bounds the summed footprint of admitted requests;
+ * `num_slots` streams run requests concurrently. */
+MGPU_API mgpu_status_t mgpu_server_create(int device, size_t budget_bytes, int num_slots,
+  mgpu_server_t** out);
+/* Queues a request; MGPU_ERR_BUDGET if its footprint alone exceeds the
+ * budget.  *id identifies it for poll / wait. */
+MGPU_API mgpu_status_t mgpu_server_submit(mgpu_server_t* server, const mgpu_request_t* request,
+  uint64_t* id);
+/* MGPU_OK when done, MGPU_ERR_NOT_READY while queued or running, or the
+ * request's error.  A poll that reports completion, or a wait, releases the
+ * id; a released id is MGPU_ERR_INVALID_ARG. */
+MGPU_API mgpu_status_t mgpu_server_poll(mgpu_server_t* server, uint64_t id);
+/* Blocks until the request completes; *latency_ms (optional) = submit to
+ * completion. */
+MGPU_API mgpu_status_t mgpu_server_wait(mgpu_server_t* server, uint64_t id, double* latency_ms);
+/* Blocks until every submitted request has completed. */
+MGPU_API mgpu_status_t mgpu_server_drain(mgpu_server_t* server);
+MGPU_API mgpu_status_t mgpu_server_stats(mgpu_server_t* server, mgpu_server_stats_t* out);
+/* Resets the latency record (not the requests). */
+MGPU_API mgpu_status_t mgpu_server_reset_stats(mgpu_server_t* server);
+MGPU_API mgpu_status_t mgpu_server_destroy(mgpu_server_t* server);
+
 /* ---- launch profiling (no reference counterpart; the reference times
  * whole command buffers with clock_gettime, examples/vk_radix/vk_radix.cxx:
  * 51-63).  When enabled, every kernel the library launches on this context

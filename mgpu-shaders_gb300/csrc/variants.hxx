@@ -16,11 +16,13 @@ inline const char* radix_name(int key_bytes, int v) {
   return key_bytes == 4 ? n4[v] : n8[v];
 }
 
-// scan / reduce: 4-byte {256x16, 256x8, 512x16}; 8-byte {256x8, 512x8}.
-inline int scan_count(int bytes) { return bytes == 4 ? 3 : 2; }
+// scan: threads x elements per thread, s = pipeline stages (s0: one tile per
+// CTA), k = look-back statuses per lane.
+inline int scan_count(int bytes) { return bytes == 4 ? 6 : 4; }
 inline const char* scan_name(int bytes, int v) {
-  static const char* n4[] = { "256x16", "256x8", "512x16" };
-  static const char* n8[] = { "256x8", "512x8" };
+  static const char* n4[] = { "256x32s0k1", "256x32s2k1", "256x16s3k1", "256x32s3k1",
+    "512x32s0k1", "256x32s0k2" };
+  static const char* n8[] = { "256x16s0k1", "256x16s2k1", "256x8s3k1", "512x16s0k1" };
   return bytes == 4 ? n4[v] : n8[v];
 }
 

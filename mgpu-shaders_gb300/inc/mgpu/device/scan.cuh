@@ -111,46 +111,64 @@ struct tile_status_t<T, true> {
 };
 
 // Warp 0 of a tile: returns the exclusive prefix of all earlier tiles (which
-// already include `init` through tile 0's inclusive value).  Walks back 32
-// tiles per step; lane i looks at tile (base - i).
-template<typename T, typename op_t, typename status_t>
+// already include `init` through tile 0's inclusive value).  One window of
+// 32 * K predecessors is read per round trip to L2: lane l reads tiles
+// base - (l * K + q), q = 0..K-1, nearest first.  The window's statuses up to
+// the nearest inclusive one are combined; if any of those is not yet
+// published, the window is read again.  Tiles arrive every few nanoseconds,
+// so a window must reach back past every tile still in its own look-back
+// (their number is about the look-back latency over the tile interval) for
+// the look-back to end in one round trip.
+template<int K, typename T, typename op_t, typename status_t>
 __device__ T lookback_warp(const status_t& st, int64_t tile, op_t op, int* error) {
   const int lane = threadIdx.x & 31;
   T acc = op_t::identity();
   bool have = false;
   int64_t base = tile - 1;
+  int spins = 0;
   while(true) {
-    int64_t j = base - lane;
-    T v = op_t::identity();
-    uint32_t flag = status_inclusive;
-    if(j >= 0) {
-      int spins = 0;
-      while(true) {
-        flag = st.read(j, v);
-        if(flag != status_invalid) break;
-        if(++spins >= spin_limit ||
-           (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
-          raise_error(error, err_lookback_timeout);
-          flag = status_inclusive;
-          v = op_t::identity();
-          break;
-        }
-      }
+    T v[K];
+    uint32_t f[K];
+#pragma unroll
+    for(int q = 0; q < K; ++q) {
+      int64_t j = base - (lane * K + q);
+      v[q] = op_t::identity();
+      f[q] = status_inclusive;
+      if(j >= 0) f[q] = st.read(j, v[q]);
     }
-    uint32_t inc_mask = __ballot_sync(0xffffffffu, flag == status_inclusive);
-    int limit = inc_mask ? __ffs(inc_mask) - 1 : 31;
-    // Ordered reduction of lanes [0, limit]: the earlier tile (higher lane)
-    // is the left operand.
+    int qinc = K;
+#pragma unroll
+    for(int q = K - 1; q >= 0; --q) if(f[q] == status_inclusive) qinc = q;
+    const uint32_t inc_mask = __ballot_sync(0xffffffffu, qinc < K);
+    const int limit = inc_mask ? __ffs(inc_mask) - 1 : 31;
+    // Positions nearer than the first inclusive status (and that one) count.
+    const int q_end = lane < limit ? K : (lane == limit ? (inc_mask ? qinc + 1 : K) : 0);
+    bool missing = false;
+#pragma unroll
+    for(int q = 0; q < K; ++q) if(q < q_end && f[q] == status_invalid) missing = true;
+    if(__any_sync(0xffffffffu, missing)) {
+      if(++spins >= spin_limit ||
+         (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
+        raise_error(error, err_lookback_timeout);
+        return acc;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    // The lane's statuses, earlier tiles (larger q) as left operands.
+    T lv = op_t::identity();
+#pragma unroll
+    for(int q = 0; q < K; ++q) if(q < q_end) lv = op(v[q], lv);
 #pragma unroll
     for(int off = 1; off < 32; off <<= 1) {
-      T y = __shfl_down_sync(0xffffffffu, v, off);
-      if(lane + off <= limit) v = op(y, v);
+      T y = __shfl_down_sync(0xffffffffu, lv, off);
+      if(lane + off <= limit) lv = op(y, lv);
     }
-    T r = __shfl_sync(0xffffffffu, v, 0);
+    T r = __shfl_sync(0xffffffffu, lv, 0);
     acc = have ? op(r, acc) : r;
     have = true;
     if(inc_mask) return acc;
-    base -= 32;
+    base -= 32 * K;
   }
 }
 
@@ -207,14 +225,74 @@ __device__ __forceinline__ void store_thread(T* dst, int valid_here, bool vec, c
   }
 }
 
-template<typename T, typename op_t, int NT, int VT, bool exclusive>
+// Warp-striped vector layout of a tile: warp w owns elements
+// [w * 32 * VT, (w + 1) * 32 * VT) of the tile; in row r of that range lane l
+// holds the PER = 16 / sizeof(T) consecutive elements starting at
+// (r * 32 + l) * PER, so each warp load or store instruction moves 512
+// contiguous bytes.  `valid` elements of the tile exist; the rest read as
+// `fill`.
+template<typename T, int VT>
+struct striped_t {
+  static constexpr int PER = 16 / (int)sizeof(T);
+  static constexpr int ROWS = VT / PER;
+  static_assert(VT % PER == 0, "elements per thread must fill 16-byte vectors");
+  static __device__ __forceinline__ int offset(int warp, int lane, int r) {
+    return warp * 32 * VT + (r * 32 + lane) * PER;
+  }
+  static __device__ __forceinline__ void load(const T* tile, int valid, bool vec, int warp,
+    int lane, T (&x)[VT], T fill) {
+    if(vec) {
+      uint4 w[ROWS];
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r)
+        w[r] = __ldcs(reinterpret_cast<const uint4*>(tile + offset(warp, lane, r)));
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) memcpy(&x[r * PER], &w[r], 16);
+    } else {
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r)
+#pragma unroll
+        for(int j = 0; j < PER; ++j) {
+          int e = offset(warp, lane, r) + j;
+          x[r * PER + j] = e < valid ? tile[e] : fill;
+        }
+    }
+  }
+  static __device__ __forceinline__ void store(T* tile, int valid, bool vec, int warp, int lane,
+    const T (&x)[VT]) {
+    if(vec) {
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        uint4 w;
+        memcpy(&w, &x[r * PER], 16);
+        __stcs(reinterpret_cast<uint4*>(tile + offset(warp, lane, r)), w);
+      }
+    } else {
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r)
+#pragma unroll
+        for(int j = 0; j < PER; ++j) {
+          int e = offset(warp, lane, r) + j;
+          if(e < valid) tile[e] = x[r * PER + j];
+        }
+    }
+  }
+};
+
+// One tile per CTA (tile ids from an atomic counter, so every tile that is
+// waited on belongs to a CTA that is already running).  The tile is loaded in
+// the warp-striped layout and each warp scans its range in registers; warp 0
+// scans the warp totals, publishes the tile aggregate and looks back; the
+// carry-in is added and the tile stored with the same striped layout.
+template<typename T, typename op_t, int NT, int VT, bool exclusive, int LBK = 1>
 __global__ void __launch_bounds__(NT)
 scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
   uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
+  typedef striped_t<T, VT> S;
+  constexpr int PER = S::PER, ROWS = S::ROWS;
   constexpr int TILE = NT * VT;
   constexpr int NW = NT / 32;
   __shared__ T warp_tot[NW];
-  __shared__ T s_prefix;
   __shared__ int64_t s_tile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if(tid == 0) s_tile = atomicAdd(tile_counter, 1u);
@@ -223,51 +301,188 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   const int64_t base = tile * TILE;
   const int valid = (int)min((int64_t)TILE, count - base);
   const bool vec = vec_ok && valid == TILE;
-  const int valid_here = valid - tid * VT;
 
   T x[VT];
-  load_thread<T, VT>(in + base + tid * VT, valid_here, vec, x, op_t::identity());
-#pragma unroll
-  for(int i = 1; i < VT; ++i) x[i] = op(x[i - 1], x[i]);
+  S::load(in + base, valid, vec, warp, lane, x, op_t::identity());
 
-  T winc = warp_inclusive_scan(x[VT - 1], op);
-  T wexc = __shfl_up_sync(0xffffffffu, winc, 1);
-  if(lane == 31) warp_tot[warp] = winc;
+  // Warp-local scan, row by row: within each 16-byte vector, then across the
+  // lanes' vector totals, then the carry of the earlier rows.
+  T acc = op_t::identity();
+#pragma unroll
+  for(int r = 0; r < ROWS; ++r) {
+    T v[PER];
+#pragma unroll
+    for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], x[r * PER + j]) : x[r * PER];
+    T linc = warp_inclusive_scan(v[PER - 1], op);
+    T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
+    if(lane == 0) lexc = op_t::identity();
+    T row_carry = op(acc, lexc);
+    if(exclusive) {
+#pragma unroll
+      for(int j = 0; j < PER; ++j) x[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
+    } else {
+#pragma unroll
+      for(int j = 0; j < PER; ++j) x[r * PER + j] = op(row_carry, v[j]);
+    }
+    acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
+  }
+  if(lane == 0) warp_tot[warp] = acc;
   __syncthreads();
   if(warp == 0) {
     T t = lane < NW ? warp_tot[lane] : op_t::identity();
-    t = warp_inclusive_scan(t, op);
-    if(lane < NW) warp_tot[lane] = t;
-  }
-  __syncthreads();
-  const T tile_agg = warp_tot[NW - 1];
-  T thread_excl = lane ? wexc : op_t::identity();
-  if(warp) thread_excl = op(warp_tot[warp - 1], thread_excl);
-
-  if(warp == 0) {
+    T tinc = warp_inclusive_scan(t, op);
+    const T tile_agg = __shfl_sync(0xffffffffu, tinc, NW - 1);
     T prefix;
     if(tile == 0) {
       prefix = init;
       if(lane == 0) st.publish(0, status_inclusive, op(init, tile_agg));
     } else {
       if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
-      prefix = lookback_warp<T>(st, tile, op, error);
+      prefix = lookback_warp<LBK, T>(st, tile, op, error);
       if(lane == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
     }
-    if(lane == 0) s_prefix = prefix;
+    T texc = __shfl_up_sync(0xffffffffu, tinc, 1);
+    if(lane < NW) warp_tot[lane] = lane ? op(prefix, texc) : prefix;
+    if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
   }
   __syncthreads();
-  const T carry = op(s_prefix, thread_excl);
-  if(exclusive) {
+  const T carry = warp_tot[warp];
 #pragma unroll
-    for(int i = VT - 1; i > 0; --i) x[i] = op(carry, x[i - 1]);
-    x[0] = carry;
-  } else {
+  for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
+  S::store(out + base, valid, vec, warp, lane, x);
+}
+
+// Persistent, software-pipelined form of scan_kernel.  A grid of resident
+// CTAs takes tile ids from the atomic counter STAGES at a time ahead: each
+// held tile is copied into its own shared-memory stage by one bulk (TMA)
+// copy as soon as its id is known, so while a CTA scans a tile and waits on
+// its look-back, the loads of its next STAGES - 1 tiles are in flight.  A CTA
+// processes its tiles in the order it took them (increasing ids), so every
+// tile that a look-back waits on belongs to a running CTA that finishes its
+// earlier tiles first.  Tiles that cannot be bulk-copied (the ragged last
+// tile, or unaligned pointers) are read from global memory directly.
+template<typename T, int NT, int VT, int STAGES>
+struct scan_pipe_layout {
+  static constexpr int TILE = NT * VT;
+  static constexpr size_t stage_bytes = sizeof(T) * TILE;
+  static constexpr size_t bar_off = STAGES * stage_bytes;
+  static constexpr size_t bytes = bar_off + 8 * STAGES;
+};
+
+template<typename T, typename op_t, int NT, int VT, int STAGES, bool exclusive, int LBK = 1>
+__global__ void __launch_bounds__(NT)
+scan_pipe_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
+  uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
+  typedef striped_t<T, VT> S;
+  typedef scan_pipe_layout<T, NT, VT, STAGES> L;
+  constexpr int PER = S::PER, ROWS = S::ROWS;
+  constexpr int TILE = NT * VT;
+  constexpr int NW = NT / 32;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
+  __shared__ T warp_tot[NW];
+  __shared__ int64_t s_tile[STAGES];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  static_assert(NW >= 2, "the refill thread is outside warp 0");
+  const int64_t num_tiles = div_up(count, TILE);
+  const int64_t bulk_tiles = vec_ok ? count / TILE : 0;    // whole, aligned tiles
+  // Lane 0 of the last warp takes tile ids and issues the copies, so that
+  // warp 0's look-back never waits on the id atomic.
+  const int refill_tid = NT - 32;
+
+  // Records tile `id` for `stage` and starts its copy.
+  auto refill = [&](int stage, int64_t id) {
+    s_tile[stage] = id;
+    if(id < bulk_tiles) {
+      mbar_arrive_expect_tx(bar + stage, (uint32_t)L::stage_bytes);
+      bulk_load(smem + stage * L::stage_bytes, in + id * TILE, (uint32_t)L::stage_bytes,
+        bar + stage);
+    }
+  };
+  if(tid == refill_tid) {
+#pragma unroll
+    for(int s = 0; s < STAGES; ++s) mbar_init(bar + s, 1);
+    fence_mbar_init();
+#pragma unroll
+    for(int s = 0; s < STAGES; ++s) refill(s, atomicAdd(tile_counter, 1u));
+  }
+  __syncthreads();
+
+  for(int k = 0;; ++k) {
+    // The id for the stage this iteration frees; its atomic overlaps the
+    // iteration's work.
+    int64_t next_id = 0;
+    if(tid == refill_tid) next_id = atomicAdd(tile_counter, 1u);
+    const int stage = k % STAGES;
+    const uint32_t parity = (uint32_t)(k / STAGES) & 1;
+    const int64_t tile = s_tile[stage];
+    if(tile >= num_tiles) break;
+    const int64_t base = tile * TILE;
+    const int valid = (int)min((int64_t)TILE, count - base);
+    const bool vec = vec_ok && valid == TILE;
+    T x[VT];
+    if(tile < bulk_tiles) {
+      // A timed-out wait has raised the error; the stage is read anyway so
+      // that the tile still publishes and no successor waits on it.
+      mbar_wait_bounded(bar + stage, parity, error);
+      const T* s_in = (const T*)(smem + stage * L::stage_bytes);
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        uint4 w = *reinterpret_cast<const uint4*>(s_in + S::offset(warp, lane, r));
+        memcpy(&x[r * PER], &w, 16);
+      }
+    } else {
+      S::load(in + base, valid, vec, warp, lane, x, op_t::identity());
+    }
+
+    T acc = op_t::identity();
+#pragma unroll
+    for(int r = 0; r < ROWS; ++r) {
+      T v[PER];
+#pragma unroll
+      for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], x[r * PER + j]) : x[r * PER];
+      T linc = warp_inclusive_scan(v[PER - 1], op);
+      T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
+      if(lane == 0) lexc = op_t::identity();
+      T row_carry = op(acc, lexc);
+      if(exclusive) {
+#pragma unroll
+        for(int j = 0; j < PER; ++j) x[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
+      } else {
+#pragma unroll
+        for(int j = 0; j < PER; ++j) x[r * PER + j] = op(row_carry, v[j]);
+      }
+      acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
+    }
+    if(lane == 0) warp_tot[warp] = acc;
+    __syncthreads();                 // stage consumed; warp totals visible
+    // The stage is free: start the copy of the tile STAGES ahead.
+    if(tid == refill_tid) refill(stage, next_id);
+    if(warp == 0) {
+      T t = lane < NW ? warp_tot[lane] : op_t::identity();
+      T tinc = warp_inclusive_scan(t, op);
+      const T tile_agg = __shfl_sync(0xffffffffu, tinc, NW - 1);
+      T prefix;
+      if(tile == 0) {
+        prefix = init;
+        if(lane == 0) st.publish(0, status_inclusive, op(init, tile_agg));
+      } else {
+        if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
+        prefix = lookback_warp<LBK, T>(st, tile, op, error);
+        if(lane == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
+      }
+      T texc = __shfl_up_sync(0xffffffffu, tinc, 1);
+      if(lane < NW) warp_tot[lane] = lane ? op(prefix, texc) : prefix;
+      if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
+    }
+    __syncthreads();
+    const T carry = warp_tot[warp];
 #pragma unroll
     for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
+    S::store(out + base, valid, vec, warp, lane, x);
   }
-  store_thread<T, VT>(out + base + tid * VT, valid_here, vec, x);
-  if(reduction && tid == 0 && base + TILE >= count) *reduction = op(s_prefix, tile_agg);
+  // Copies started for ids past the end were never issued (bulk_tiles <=
+  // num_tiles), so no copy is in flight here.
 }
 
 template<typename T>
@@ -291,7 +506,7 @@ reduce_kernel(const T* in, int64_t count, T init, op_t op, T* partials, uint32_t
     const int64_t base = tile * TILE;
     const int valid = (int)min((int64_t)TILE, count - base);
     T x[VT];
-    load_thread<T, VT>(in + base + tid * VT, valid - tid * VT, vec_ok && valid == TILE, x,
+    striped_t<T, VT>::load(in + base, valid, vec_ok && valid == TILE, warp, lane, x,
       op_t::identity());
 #pragma unroll
     for(int i = 0; i < VT; ++i) acc = op(acc, x[i]);

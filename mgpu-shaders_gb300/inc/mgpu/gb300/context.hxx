@@ -185,6 +185,19 @@ struct context_t {
     return true;
   }
 
+  // CTAs of `kernel` resident per SM at `nt` threads and `smem` dynamic
+  // shared bytes (cached per kernel and device); 0 on error.
+  template<typename kernel_t>
+  int resident_ctas(kernel_t kernel, int nt, size_t smem) {
+    auto key = std::make_pair((const void*)kernel, device);
+    auto it = occupancy.find(key);
+    if(it != occupancy.end()) return it->second;
+    int n = 0;
+    if(check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, nt, smem))) return 0;
+    occupancy[key] = n;
+    return n;
+  }
+
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
@@ -205,6 +218,7 @@ struct context_t {
   std::vector<cudaEvent_t> event_pool;
   std::map<std::string, std::pair<int64_t, double>> profile;
   std::set<std::pair<const void*, int>> smem_configured;
+  std::map<std::pair<const void*, int>, int> occupancy;
 };
 
 // Source compatibility with code written against cmd_buffer_t

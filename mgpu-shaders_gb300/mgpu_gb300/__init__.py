@@ -302,3 +302,131 @@ class Graph:
 
 def build_dir():
     return os.path.dirname(library_path())
+
+
+class Request(ctypes.Structure):
+    """mgpu_request_t."""
+    _fields_ = [("op", ctypes.c_int), ("key_type", ctypes.c_int), ("val_bytes", ctypes.c_int),
+                ("count", ctypes.c_int64), ("count_b", ctypes.c_int64),
+                ("keys", ctypes.c_void_p), ("vals", ctypes.c_void_p),
+                ("keys_b", ctypes.c_void_p), ("vals_b", ctypes.c_void_p),
+                ("out_keys", ctypes.c_void_p), ("out_vals", ctypes.c_void_p),
+                ("scan_type", ctypes.c_int), ("op_arg", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    """mgpu_server_stats_t."""
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("elements", ctypes.c_int64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("peak_bytes", ctypes.c_size_t)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+REQ_OPS = {"sort": 0, "merge": 1, "scan": 2}
+
+
+def _host_ptr(a):
+    """Address of a C-contiguous numpy array or CPU torch tensor (None -> 0)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous:
+            raise ValueError("host buffers must be C-contiguous")
+        return a.ctypes.data
+    if a.device.type != "cpu" or not a.is_contiguous():
+        raise ValueError("host buffers must be contiguous CPU tensors")
+    return a.data_ptr()
+
+
+def _np_dtype(a):
+    if isinstance(a, np.ndarray):
+        return a.dtype
+    return np.dtype(str(a.dtype).replace("torch.", ""))
+
+
+class Server:
+    """mgpu_server_t: queued sort / merge / scan requests on host buffers,
+    admitted under an HBM budget and run concurrently on `num_slots` streams.
+    Host buffers are referenced until the request has been waited on; pinned
+    buffers (torch `pin_memory()`) give asynchronous copies."""
+
+    def __init__(self, device=0, budget_bytes=8 << 30, num_slots=4):
+        self._h = ctypes.c_void_p()
+        _lib.check(lib().mgpu_server_create(device, budget_bytes, num_slots,
+                                            ctypes.byref(self._h)), None)
+        self._held = {}
+
+    def close(self):
+        if self._h:
+            lib().mgpu_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._held.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, req, held=()):
+        """Queues a filled-in Request; `held` objects stay referenced until
+        the request is waited on."""
+        rid = ctypes.c_uint64()
+        _lib.check(lib().mgpu_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)), None)
+        self._held[rid.value] = held
+        return rid.value
+
+    def submit_sort(self, keys, vals, out_keys, out_vals):
+        req = Request(op=0, key_type=DTYPES[_np_dtype(keys)],
+                      val_bytes=0 if vals is None else _np_dtype(vals).itemsize,
+                      count=len(keys), keys=_host_ptr(keys), vals=_host_ptr(vals),
+                      out_keys=_host_ptr(out_keys), out_vals=_host_ptr(out_vals))
+        return self.submit(req, (keys, vals, out_keys, out_vals))
+
+    def submit_merge(self, a_keys, a_vals, b_keys, b_vals, out_keys, out_vals, comp="less"):
+        req = Request(op=1, key_type=DTYPES[_np_dtype(a_keys)],
+                      val_bytes=0 if a_vals is None else _np_dtype(a_vals).itemsize,
+                      count=len(a_keys), count_b=len(b_keys),
+                      keys=_host_ptr(a_keys), vals=_host_ptr(a_vals),
+                      keys_b=_host_ptr(b_keys), vals_b=_host_ptr(b_vals),
+                      out_keys=_host_ptr(out_keys), out_vals=_host_ptr(out_vals),
+                      op_arg=COMPS[comp])
+        return self.submit(req, (a_keys, a_vals, b_keys, b_vals, out_keys, out_vals))
+
+    def submit_scan(self, data, out, scan_type="exc", op="plus"):
+        req = Request(op=2, key_type=DTYPES[_np_dtype(data)], count=len(data),
+                      keys=_host_ptr(data), out_keys=_host_ptr(out),
+                      scan_type=SCAN_TYPES[scan_type], op_arg=OPS[op])
+        return self.submit(req, (data, out))
+
+    def poll(self, rid):
+        """True when done (releases the id), False while queued or running."""
+        rc = lib().mgpu_server_poll(self._h, rid)
+        if rc == 7:
+            return False
+        self._held.pop(rid, None)
+        _lib.check(rc, None)
+        return True
+
+    def wait(self, rid):
+        """Blocks until the request is done; returns its latency in ms."""
+        lat = ctypes.c_double()
+        rc = lib().mgpu_server_wait(self._h, rid, ctypes.byref(lat))
+        self._held.pop(rid, None)
+        _lib.check(rc, None)
+        return lat.value
+
+    def drain(self):
+        _lib.check(lib().mgpu_server_drain(self._h), None)
+
+    def stats(self):
+        s = ServerStats()
+        _lib.check(lib().mgpu_server_stats(self._h, ctypes.byref(s)), None)
+        return s.as_dict()
+
+    def reset_stats(self):
+        _lib.check(lib().mgpu_server_reset_stats(self._h), None)

@@ -66,6 +66,14 @@ _SIGS = {
     "mgpu_graph_launch": ([_VP, _VP], _I32),
     "mgpu_graph_destroy": ([_VP], _I32),
     "mgpu_cache_reserve": ([_VP, ctypes.c_size_t], _I32),
+    "mgpu_server_create": ([_I32, ctypes.c_size_t, _I32, _VP], _I32),
+    "mgpu_server_submit": ([_VP, _VP, _VP], _I32),
+    "mgpu_server_poll": ([_VP, ctypes.c_uint64], _I32),
+    "mgpu_server_wait": ([_VP, ctypes.c_uint64, _VP], _I32),
+    "mgpu_server_drain": ([_VP], _I32),
+    "mgpu_server_stats": ([_VP, _VP], _I32),
+    "mgpu_server_reset_stats": ([_VP], _I32),
+    "mgpu_server_destroy": ([_VP], _I32),
     "mgpu_profile_enable": ([_VP, _I32], _I32),
     "mgpu_profile_read": ([_VP, _VP, ctypes.c_size_t, _VP, _VP, _I32, _VP], _I32),
     "mgpu_launch_count": ([_VP], _I64),

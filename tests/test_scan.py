@@ -158,3 +158,34 @@ def test_scan_f32_full_size(mgpu, ctx, oracle):
     err = np.abs(got.astype(np.float64) - ref)
     bound = F32_REL * ref_abs + F32_ABS
     assert np.all(err <= bound), float(np.max(err / bound))
+
+
+@pytest.mark.parametrize("dt", [np.int32, np.int64])
+@pytest.mark.parametrize("scan_type", ["exc", "inc"])
+def test_scan_every_variant_unaligned_and_ragged(mgpu, ctx, oracle, rng, dt, scan_type):
+    """Every launch shape, with 16-byte-aligned pointers (bulk-copied tiles)
+    and with pointers one element off (tiles read element by element), at
+    sizes that end in a ragged tile."""
+    import torch
+    itemsize = np.dtype(dt).itemsize
+    names = ctx.tuning_variants("scan", dt)
+    try:
+        for var in range(len(names)):
+            ctx.tuning_set("scan", dt, 0, -1, var)
+            for n in (70_001, 1_000_003):
+                x = ints(rng, n, dt, hi=1 << 20)
+                ref = oracle.scan_int(x, exclusive=scan_type == "exc")
+                for shift in (0, 1):
+                    src = mgpu.DeviceArray(n + 1, dt)
+                    dst = mgpu.DeviceArray(n + 1, dt)
+                    din = mgpu.DeviceArray(n, dt, tensor=src.tensor[shift * itemsize:])
+                    dout = mgpu.DeviceArray(n, dt, tensor=dst.tensor[shift * itemsize:])
+                    din.tensor[: n * itemsize].copy_(torch.from_numpy(x.view(np.uint8)))
+                    red = mgpu.DeviceArray(1, dt)
+                    ctx.scan(din, dout, scan_type=scan_type, reduction=red)
+                    ctx.synchronize()
+                    assert np.array_equal(dout.numpy(), ref), (names[var], n, shift)
+                    total = x.astype(np.int64).sum().astype(dt)
+                    assert red.numpy()[0] == total, (names[var], n, shift)
+    finally:
+        ctx.tuning_set("scan", dt, 0, -1, 0)
