@@ -16,13 +16,12 @@ inline const char* radix_name(int key_bytes, int v) {
   return key_bytes == 4 ? n4[v] : n8[v];
 }
 
-// scan: threads x elements per thread, s = pipeline stages (s0: one tile per
-// CTA), k = look-back statuses per lane.
-inline int scan_count(int bytes) { return bytes == 4 ? 6 : 4; }
+// scan: threads x elements per thread, b = CTAs per SM; "p" = persistent
+// with deferred look-back, "t" = one tile per CTA.
+inline int scan_count(int) { return 4; }
 inline const char* scan_name(int bytes, int v) {
-  static const char* n4[] = { "256x32s0k1", "256x32s2k1", "256x16s3k1", "256x32s3k1",
-    "512x32s0k1", "256x32s0k2" };
-  static const char* n8[] = { "256x16s0k1", "256x16s2k1", "256x8s3k1", "512x16s0k1" };
+  static const char* n4[] = { "256x32b4p", "512x32b2p", "256x16b6p", "256x32b4t" };
+  static const char* n8[] = { "512x16b2p", "256x16b4p", "256x8b6p", "256x16b4t" };
   return bytes == 4 ? n4[v] : n8[v];
 }
 

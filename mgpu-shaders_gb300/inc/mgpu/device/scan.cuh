@@ -5,10 +5,11 @@
 // one CTA looping over <= 8 tiles or an upsweep reduce / recursive scan of the
 // partials / downsweep with carry-in: three launches per recursion level and
 // 12 bytes of traffic per 4-byte element.  Here one launch reads each element
-// once and writes it once (8 B/elem): each CTA takes the next tile id from an
-// atomic counter, scans its tile in registers, publishes its aggregate, and
-// warp 0 walks back over predecessor tiles 32 at a time until it meets an
-// inclusive prefix.  The same kernel serves every size.
+// once and writes it once (8 B/elem) with a decoupled look-back over tiles
+// whose ids come from an atomic counter (scan_defer_kernel: resident CTAs
+// that publish a tile's aggregate in one iteration and look back, scan and
+// store it in the next; scan_kernel: one tile per CTA, used where a
+// persistent grid is not wanted).
 //
 // Operators carry their identity (used for padding and lane 0 of an
 // exclusive warp scan); integer addition wraps in two's complement, as the
@@ -172,6 +173,76 @@ __device__ T lookback_warp(const status_t& st, int64_t tile, op_t op, int* error
   }
 }
 
+// All NW warps of a tile look back together: in each round warp w reads the
+// 32 predecessors base - (32 w + lane), so one round trip to L2 covers 32 NW
+// tiles.  (The chain of inclusive prefixes advances by about one window per
+// round trip, which bounds tiles per second; a warp-wide window of 32 limits
+// a 2^28-element scan of 8192-element tiles to about 50 tiles per
+// microsecond, half of what the HBM bandwidth asks for.)  The warps' window
+// values and flags meet in shared memory; every thread derives the same
+// result, so the return value is uniform across the CTA.  Called by every
+// thread of the CTA, with `s_val` / `s_info` of NW entries.
+template<int NW, typename T, typename op_t, typename status_t>
+__device__ T lookback_cta(const status_t& st, int64_t tile, op_t op, int* error, T* s_val,
+  int* s_info) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T acc = op_t::identity();
+  bool have = false;
+  int64_t base = tile - 1;
+  for(int round = 0;; ++round) {
+    const int64_t j = base - (warp * 32 + lane);
+    T v = op_t::identity();
+    uint32_t f = status_inclusive;
+    if(j >= 0) f = st.read(j, v);
+    const uint32_t inc_mask = __ballot_sync(0xffffffffu, f == status_inclusive);
+    const int limit = inc_mask ? __ffs(inc_mask) - 1 : 31;
+    const bool missing = __any_sync(0xffffffffu, lane <= limit && f == status_invalid);
+#pragma unroll
+    for(int off = 1; off < 32; off <<= 1) {
+      T y = __shfl_down_sync(0xffffffffu, v, off);
+      if(lane + off <= limit) v = op(y, v);
+    }
+    if(lane == 0) {
+      int info = (inc_mask ? 1 : 0) | (missing ? 2 : 0);
+      // Give up (uniformly, through shared memory) after the spin limit or
+      // when another CTA has raised the error.
+      if(warp == 0 && round &&
+         (round >= spin_limit || (0 == (round & (spin_poll_error - 1)) && error_raised(error))))
+        info |= 4;
+      s_val[warp] = v;
+      s_info[warp] = info;
+    }
+    __syncthreads();
+    if(s_info[0] & 4) {
+      raise_error(error, err_lookback_timeout);
+      return acc;
+    }
+    bool miss = false;
+    int w_last = NW - 1, found = 0;
+#pragma unroll
+    for(int w = 0; w < NW; ++w) {
+      const int info = s_info[w];
+      if(!found && !miss) {
+        if(info & 2) miss = true;
+        else if(info & 1) { w_last = w; found = 1; }
+      }
+    }
+    T r = op_t::identity();
+    if(!miss) {
+      for(int w = w_last; w >= 0; --w) r = op(r, s_val[w]);
+    }
+    __syncthreads();                       // s_val / s_info are rewritten next round
+    if(miss) {
+      __nanosleep(32);
+      continue;
+    }
+    acc = have ? op(r, acc) : r;
+    have = true;
+    if(found) return acc;
+    base -= 32 * NW;
+  }
+}
+
 template<typename T, typename op_t>
 __device__ __forceinline__ T warp_inclusive_scan(T x, op_t op) {
   const int lane = threadIdx.x & 31;
@@ -284,8 +355,8 @@ struct striped_t {
 // the warp-striped layout and each warp scans its range in registers; warp 0
 // scans the warp totals, publishes the tile aggregate and looks back; the
 // carry-in is added and the tile stored with the same striped layout.
-template<typename T, typename op_t, int NT, int VT, bool exclusive, int LBK = 1>
-__global__ void __launch_bounds__(NT)
+template<typename T, typename op_t, int NT, int VT, bool exclusive, int LBK = 1, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB)
 scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
   uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
   typedef striped_t<T, VT> S;
@@ -328,136 +399,30 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   }
   if(lane == 0) warp_tot[warp] = acc;
   __syncthreads();
-  if(warp == 0) {
-    T t = lane < NW ? warp_tot[lane] : op_t::identity();
-    T tinc = warp_inclusive_scan(t, op);
-    const T tile_agg = __shfl_sync(0xffffffffu, tinc, NW - 1);
+  T carry;
+  if constexpr(LBK == 0) {
+    // Every thread derives the tile aggregate and its warp's offset.
+    __shared__ T s_val[NW];
+    __shared__ int s_info[NW];
+    T wexc = op_t::identity(), tile_agg = op_t::identity();
+#pragma unroll
+    for(int w = 0; w < NW; ++w) {
+      const T t = warp_tot[w];
+      if(w < warp) wexc = op(wexc, t);
+      tile_agg = op(tile_agg, t);
+    }
     T prefix;
     if(tile == 0) {
       prefix = init;
-      if(lane == 0) st.publish(0, status_inclusive, op(init, tile_agg));
+      if(tid == 0) st.publish(0, status_inclusive, op(init, tile_agg));
     } else {
-      if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
-      prefix = lookback_warp<LBK, T>(st, tile, op, error);
-      if(lane == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
+      if(tid == 0) st.publish(tile, status_aggregate, tile_agg);
+      prefix = lookback_cta<NW, T>(st, tile, op, error, s_val, s_info);
+      if(tid == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
     }
-    T texc = __shfl_up_sync(0xffffffffu, tinc, 1);
-    if(lane < NW) warp_tot[lane] = lane ? op(prefix, texc) : prefix;
-    if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
-  }
-  __syncthreads();
-  const T carry = warp_tot[warp];
-#pragma unroll
-  for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
-  S::store(out + base, valid, vec, warp, lane, x);
-}
-
-// Persistent, software-pipelined form of scan_kernel.  A grid of resident
-// CTAs takes tile ids from the atomic counter STAGES at a time ahead: each
-// held tile is copied into its own shared-memory stage by one bulk (TMA)
-// copy as soon as its id is known, so while a CTA scans a tile and waits on
-// its look-back, the loads of its next STAGES - 1 tiles are in flight.  A CTA
-// processes its tiles in the order it took them (increasing ids), so every
-// tile that a look-back waits on belongs to a running CTA that finishes its
-// earlier tiles first.  Tiles that cannot be bulk-copied (the ragged last
-// tile, or unaligned pointers) are read from global memory directly.
-template<typename T, int NT, int VT, int STAGES>
-struct scan_pipe_layout {
-  static constexpr int TILE = NT * VT;
-  static constexpr size_t stage_bytes = sizeof(T) * TILE;
-  static constexpr size_t bar_off = STAGES * stage_bytes;
-  static constexpr size_t bytes = bar_off + 8 * STAGES;
-};
-
-template<typename T, typename op_t, int NT, int VT, int STAGES, bool exclusive, int LBK = 1>
-__global__ void __launch_bounds__(NT)
-scan_pipe_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
-  uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
-  typedef striped_t<T, VT> S;
-  typedef scan_pipe_layout<T, NT, VT, STAGES> L;
-  constexpr int PER = S::PER, ROWS = S::ROWS;
-  constexpr int TILE = NT * VT;
-  constexpr int NW = NT / 32;
-  extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
-  __shared__ T warp_tot[NW];
-  __shared__ int64_t s_tile[STAGES];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  static_assert(NW >= 2, "the refill thread is outside warp 0");
-  const int64_t num_tiles = div_up(count, TILE);
-  const int64_t bulk_tiles = vec_ok ? count / TILE : 0;    // whole, aligned tiles
-  // Lane 0 of the last warp takes tile ids and issues the copies, so that
-  // warp 0's look-back never waits on the id atomic.
-  const int refill_tid = NT - 32;
-
-  // Records tile `id` for `stage` and starts its copy.
-  auto refill = [&](int stage, int64_t id) {
-    s_tile[stage] = id;
-    if(id < bulk_tiles) {
-      mbar_arrive_expect_tx(bar + stage, (uint32_t)L::stage_bytes);
-      bulk_load(smem + stage * L::stage_bytes, in + id * TILE, (uint32_t)L::stage_bytes,
-        bar + stage);
-    }
-  };
-  if(tid == refill_tid) {
-#pragma unroll
-    for(int s = 0; s < STAGES; ++s) mbar_init(bar + s, 1);
-    fence_mbar_init();
-#pragma unroll
-    for(int s = 0; s < STAGES; ++s) refill(s, atomicAdd(tile_counter, 1u));
-  }
-  __syncthreads();
-
-  for(int k = 0;; ++k) {
-    // The id for the stage this iteration frees; its atomic overlaps the
-    // iteration's work.
-    int64_t next_id = 0;
-    if(tid == refill_tid) next_id = atomicAdd(tile_counter, 1u);
-    const int stage = k % STAGES;
-    const uint32_t parity = (uint32_t)(k / STAGES) & 1;
-    const int64_t tile = s_tile[stage];
-    if(tile >= num_tiles) break;
-    const int64_t base = tile * TILE;
-    const int valid = (int)min((int64_t)TILE, count - base);
-    const bool vec = vec_ok && valid == TILE;
-    T x[VT];
-    if(tile < bulk_tiles) {
-      // A timed-out wait has raised the error; the stage is read anyway so
-      // that the tile still publishes and no successor waits on it.
-      mbar_wait_bounded(bar + stage, parity, error);
-      const T* s_in = (const T*)(smem + stage * L::stage_bytes);
-#pragma unroll
-      for(int r = 0; r < ROWS; ++r) {
-        uint4 w = *reinterpret_cast<const uint4*>(s_in + S::offset(warp, lane, r));
-        memcpy(&x[r * PER], &w, 16);
-      }
-    } else {
-      S::load(in + base, valid, vec, warp, lane, x, op_t::identity());
-    }
-
-    T acc = op_t::identity();
-#pragma unroll
-    for(int r = 0; r < ROWS; ++r) {
-      T v[PER];
-#pragma unroll
-      for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], x[r * PER + j]) : x[r * PER];
-      T linc = warp_inclusive_scan(v[PER - 1], op);
-      T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
-      if(lane == 0) lexc = op_t::identity();
-      T row_carry = op(acc, lexc);
-      if(exclusive) {
-#pragma unroll
-        for(int j = 0; j < PER; ++j) x[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
-      } else {
-#pragma unroll
-        for(int j = 0; j < PER; ++j) x[r * PER + j] = op(row_carry, v[j]);
-      }
-      acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
-    }
-    if(lane == 0) warp_tot[warp] = acc;
-    __syncthreads();                 // stage consumed; warp totals visible
-    // The stage is free: start the copy of the tile STAGES ahead.
-    if(tid == refill_tid) refill(stage, next_id);
+    if(tid == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
+    carry = op(prefix, wexc);
+  } else {
     if(warp == 0) {
       T t = lane < NW ? warp_tot[lane] : op_t::identity();
       T tinc = warp_inclusive_scan(t, op);
@@ -476,13 +441,180 @@ scan_pipe_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_statu
       if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
     }
     __syncthreads();
-    const T carry = warp_tot[warp];
-#pragma unroll
-    for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
-    S::store(out + base, valid, vec, warp, lane, x);
+    carry = warp_tot[warp];
   }
-  // Copies started for ids past the end were never issued (bulk_tiles <=
-  // num_tiles), so no copy is in flight here.
+#pragma unroll
+  for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
+  S::store(out + base, valid, vec, warp, lane, x);
+}
+
+// Persistent scan with a deferred look-back (the large-input path).
+//
+// A CTA that holds its tile in registers while it looks back keeps an SM slot
+// busy for the whole look-back, and look-backs over tens of microseconds of
+// tiles take several microseconds, so a one-tile-per-CTA scan reaches only
+// about half of the HBM bandwidth.  Here each resident CTA loops over tiles
+// (ids from the atomic counter) and splits every tile's work over two
+// iterations:
+//   iteration k:   tile `cur` arrives in shared memory through one bulk copy
+//                  issued an iteration earlier; the CTA reduces it and
+//                  publishes its aggregate, then starts the copy of the next
+//                  tile into the freed stage;
+//   iteration k+1: the CTA re-reads tile `cur` from global memory (it is
+//                  still in L2), looks back (its predecessors have had an
+//                  iteration to publish), publishes its inclusive prefix at
+//                  once, scans it and stores it.
+// So a tile's data is held only in L2 while its predecessors finish, and the
+// DRAM traffic stays one read and one write per element.  Ids increase in the
+// order a CTA processes them, so every tile a look-back waits on belongs to a
+// running CTA whose earlier tiles need nothing later: the scan always
+// progresses.  Ragged or unaligned tiles are read element by element instead
+// of by bulk copy.
+template<typename T, int NT, int VT>
+struct scan_defer_layout {
+  static constexpr size_t stage_bytes = sizeof(T) * NT * VT;
+  static constexpr size_t bar_off = stage_bytes;
+  static constexpr size_t bytes = bar_off + 16;
+};
+
+template<typename T, typename op_t, int NT, int VT, bool exclusive, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
+  uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
+  typedef striped_t<T, VT> S;
+  typedef scan_defer_layout<T, NT, VT> L;
+  constexpr int PER = S::PER, ROWS = S::ROWS;
+  constexpr int TILE = NT * VT;
+  constexpr int NW = NT / 32;
+  static_assert(NW >= 2, "the copy thread is outside warp 0");
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
+  __shared__ T warp_tot[NW];
+  __shared__ T s_val[NW];
+  __shared__ int s_info[NW];
+  __shared__ int64_t s_id;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t num_tiles = div_up(count, TILE);
+  const int64_t bulk_tiles = vec_ok ? count / TILE : 0;    // whole, aligned tiles
+  const int copy_tid = NT - 32;                            // lane 0 of the last warp
+
+  // Records the id of the next tile and starts its copy (copy thread only).
+  auto fetch = [&](int64_t id) {
+    s_id = id;
+    if(id < bulk_tiles) {
+      mbar_arrive_expect_tx(bar, (uint32_t)L::stage_bytes);
+      bulk_load(smem, in + id * TILE, (uint32_t)L::stage_bytes, bar);
+    }
+  };
+  if(tid == copy_tid) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    fetch(atomicAdd(tile_counter, 1u));
+  }
+  __syncthreads();
+
+  int64_t prev = -1;
+  T prev_agg = op_t::identity(), cur_agg = op_t::identity();   // used by thread 0
+  uint32_t parity = 0;
+  while(true) {
+    // The id after `cur`; its atomic overlaps this iteration's work.
+    int64_t next_id = 0;
+    if(tid == copy_tid) next_id = atomicAdd(tile_counter, 1u);
+    const int64_t cur = s_id;
+    const bool have_cur = cur < num_tiles;
+
+    // Reduce `cur`.
+    if(have_cur) {
+      T a = op_t::identity();
+      if(cur < bulk_tiles) {
+        mbar_wait_bounded(bar, parity, error);   // a timeout raised the error
+        parity ^= 1;
+        const T* sx = (const T*)smem;
+#pragma unroll
+        for(int r = 0; r < ROWS; ++r) {
+          uint4 w = *reinterpret_cast<const uint4*>(sx + S::offset(warp, lane, r));
+          T e[PER];
+          memcpy(e, &w, 16);
+#pragma unroll
+          for(int j = 0; j < PER; ++j) a = op(a, e[j]);
+        }
+      } else {
+        T x[VT];
+        const int64_t base = cur * TILE;
+        S::load(in + base, (int)min((int64_t)TILE, count - base), false, warp, lane, x,
+          op_t::identity());
+#pragma unroll
+        for(int i = 0; i < VT; ++i) a = op(a, x[i]);
+      }
+      a = warp_reduce(a, op);
+      if(lane == 0) warp_tot[warp] = a;
+    }
+    __syncthreads();                     // the stage is consumed; warp totals visible
+    if(tid == copy_tid) fetch(next_id);
+    if(have_cur && tid == 0) {
+      T agg = op_t::identity();
+#pragma unroll
+      for(int w = 0; w < NW; ++w) agg = op(agg, warp_tot[w]);
+      if(cur == 0) st.publish(0, status_inclusive, op(init, agg));
+      else st.publish(cur, status_aggregate, agg);
+      cur_agg = agg;
+    }
+
+    // Scan and store `prev`.
+    if(prev >= 0) {
+      const int64_t base = prev * TILE;
+      const int valid = (int)min((int64_t)TILE, count - base);
+      const bool vec = vec_ok && valid == TILE;
+      T y[VT];
+      S::load(in + base, valid, vec, warp, lane, y, op_t::identity());
+      T prefix = init;
+      if(prev > 0) {
+        prefix = lookback_cta<NW, T>(st, prev, op, error, s_val, s_info);
+        // Publish at once: successors need not wait for the scan below.
+        if(tid == 0) st.publish(prev, status_inclusive, op(prefix, prev_agg));
+      } else {
+        __syncthreads();
+      }
+      T acc = op_t::identity();
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        T v[PER];
+#pragma unroll
+        for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], y[r * PER + j]) : y[r * PER];
+        T linc = warp_inclusive_scan(v[PER - 1], op);
+        T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
+        if(lane == 0) lexc = op_t::identity();
+        T row_carry = op(acc, lexc);
+        if(exclusive) {
+#pragma unroll
+          for(int j = 0; j < PER; ++j) y[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
+        } else {
+#pragma unroll
+          for(int j = 0; j < PER; ++j) y[r * PER + j] = op(row_carry, v[j]);
+        }
+        acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
+      }
+      if(lane == 0) warp_tot[warp] = acc;
+      __syncthreads();
+      T wexc = prefix, ptot = op_t::identity();
+#pragma unroll
+      for(int w = 0; w < NW; ++w) {
+        const T t = warp_tot[w];
+        if(w < warp) wexc = op(wexc, t);
+        ptot = op(ptot, t);
+      }
+      if(tid == 0 && reduction && base + TILE >= count) *reduction = op(prefix, ptot);
+#pragma unroll
+      for(int i = 0; i < VT; ++i) y[i] = op(wexc, y[i]);
+      S::store(out + base, valid, vec, warp, lane, y);
+    }
+    __syncthreads();
+    if(!have_cur) break;
+    prev = cur;
+    prev_agg = cur_agg;
+  }
+  // The stage holds no copy in flight here: ids only grow, so once `cur` is
+  // past the end the fetched id is too, and no copy was issued for it.
 }
 
 template<typename T>

@@ -21,20 +21,23 @@ template<typename T> using plus_t = device::plus_t<T>;
 template<typename T> using maximum_t = device::max_t<T>;
 template<typename T> using minimum_t = device::min_t<T>;
 
-// Launch shapes: threads, elements per thread, pipeline stages (0: one tile
-// per CTA, scan_kernel; > 0: persistent scan_pipe_kernel).
+// Launch shapes: threads, elements per thread, persistent (1: resident CTAs
+// looping over tiles with a deferred look-back, scan_defer_kernel; 0: one
+// tile per CTA, scan_kernel), CTAs per SM asked of the compiler.
 template<int bytes> struct scan_tuning;
-template<> struct scan_tuning<4> { enum { nt = 256, vt = 32, stages = 0 }; };
-template<> struct scan_tuning<8> { enum { nt = 256, vt = 16, stages = 0 }; };
+template<> struct scan_tuning<4> { enum { nt = 256, vt = 32, stages = 1, minb = 4 }; };
+template<> struct scan_tuning<8> { enum { nt = 512, vt = 16, stages = 1, minb = 2 }; };
 
 template<scan_type_t scan_type = scan_type_exc,
-  int nt = 0, int vt = 0, int stages = -1, int lbk = 1, typename T, typename op_t = plus_t<T>>
+  int nt = 0, int vt = 0, int stages = -1, int lbk = 0, int minb = -1, typename T,
+  typename op_t = plus_t<T>>
 status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
   T* out, T init = op_t::identity(), op_t op = op_t(), T* reduction = nullptr) {
   using namespace device;
   constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
   constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
   constexpr int STAGES = stages >= 0 ? stages : (int)scan_tuning<sizeof(T)>::stages;
+  constexpr int MINB = minb >= 0 ? minb : (int)scan_tuning<sizeof(T)>::minb;
   constexpr int tile = NT * VT;
   if(count < 0) return MGPU_ERR_INVALID_ARG;
   int64_t num_tiles = div_up(count, tile);
@@ -58,21 +61,20 @@ status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int
   int vec = aligned16_host(in) && aligned16_host(out);
   const char* name = scan_type == scan_type_exc ? "scan_exc" : "scan_inc";
   if constexpr(STAGES > 0) {
-    typedef scan_pipe_layout<T, NT, VT, STAGES> PL;
-    auto k = scan_pipe_kernel<T, op_t, NT, VT, STAGES, scan_type == scan_type_exc, lbk>;
-    if(!ctx.allow_smem(k, PL::bytes)) return MGPU_ERR_CUDA;
-    int per_sm = ctx.resident_ctas(k, NT, PL::bytes);
+    typedef scan_defer_layout<T, NT, VT> DL;
+    auto k = scan_defer_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, MINB>;
+    if(!ctx.allow_smem(k, DL::bytes)) return MGPU_ERR_CUDA;
+    int per_sm = ctx.resident_ctas(k, NT, DL::bytes);
     if(per_sm < 1) return MGPU_ERR_CUDA;
-    // Enough CTAs to fill the GPU, each holding STAGES tiles.
-    int64_t grid = std::min<int64_t>((int64_t)per_sm * ctx.sm_count,
-      div_up(num_tiles, STAGES));
+    // Resident CTAs only, each looping over tiles.
+    int64_t grid = std::min<int64_t>((int64_t)per_sm * ctx.sm_count, num_tiles);
     return ctx.launch(name, [&] {
-      k<<<(unsigned)std::max<int64_t>(grid, 1), NT, PL::bytes, ctx.stream>>>(in, out, count,
-        init, op, status, (uint32_t*)base, reduction, ctx.d_error, vec);
+      k<<<(unsigned)grid, NT, DL::bytes, ctx.stream>>>(in, out, count, init, op, status,
+        (uint32_t*)base, reduction, ctx.d_error, vec);
     });
   } else {
     return ctx.launch(name, [&] {
-      scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, lbk>
+      scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, lbk, MINB>
         <<<(unsigned)num_tiles, NT, 0, ctx.stream>>>(in, out, count, init, op, status,
           (uint32_t*)base, reduction, ctx.d_error, vec);
     });
