@@ -163,7 +163,10 @@ __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned c
     mbar_init(bar, 1);
     fence_mbar_init();
   }
-  for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
+  // The ballot path counts digits in the warp histograms directly; the match
+  // path keeps its counts in the warps' key slices and writes whist whole.
+  if(!L::match_in_slice)
+    for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
   __syncthreads();
   return *s_tile;
 }
@@ -326,31 +329,41 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   uint32_t r[ITEMS];
   uint32_t* wh = whist + warp * radix_bins;
   const uint32_t lt_mask = lanemask_lt();
+  // Where warp w's count of digit d sits after ranking.
+  auto warp_count = [&](int w, int d) -> uint32_t {
+    if constexpr(L::match_in_slice)
+      return ((const uint32_t*)(ks + w * 32 * ITEMS))[2 * d + 1 - ((d >> 4) & 1)];
+    else return whist[w * radix_bins + d];
+  };
   if constexpr(L::match_in_slice) {
-    // Peers through match masks: every lane ORs its lane bit into
-    // mask[digit] and reads the word back.  The masks live in this warp's own
-    // slice of the key buffer (its keys are already in registers).  Rows
-    // alternate between two banks; the lowest peer clears its entry after the
-    // row, so a bank is clean again two rows later.
-    uint32_t* mm = (uint32_t*)(ks + warp_base);
+    // Per digit, one 64-bit word in this warp's slice of the key buffer (its
+    // keys are already in registers): one half collects the row's peer mask
+    // (every lane ORs its lane bit in), the other is the warp's running
+    // count.  A lane reads both halves in one load; the lowest peer writes
+    // back the advanced count with a clear mask.  Three shared-memory
+    // operations per key.  Digits with bit 4 set keep their mask in the upper
+    // half, so the masks of any 32 digits spread over all 32 banks.
+    uint32_t* mw = (uint32_t*)(ks + warp_base);
     __syncwarp();
-    for(int j = lane; j < 2 * radix_bins; j += 32) mm[j] = 0;
+    for(int j = lane; j < 2 * radix_bins / 4; j += 32)
+      reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
     __syncwarp();
     const uint32_t lane_bit = 1u << lane;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
-      uint32_t* bank = mm + (i & 1) * radix_bins;
       const uint32_t d = extract_digit(k[i], a.shift, 8);
-      atomicOr(&bank[d], lane_bit);
+      const uint32_t hi = (d >> 4) & 1;            // mask in the upper half
+      atomicOr(&mw[2 * d + hi], lane_bit);
       __syncwarp();
-      const uint32_t peers = bank[d];
-      const uint32_t cnt = wh[d];
+      const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
       __syncwarp();
+      const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
       const uint32_t below = peers & lt_mask;
       if(!below) {
-        wh[d] = cnt + __popc(peers);
-        bank[d] = 0;
+        const uint32_t next = cnt + __popc(peers);
+        *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
       }
+      __syncwarp();
       r[i] = cnt + __popc(below);
     }
   } else {
@@ -372,15 +385,16 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
   __syncthreads();
 
-  // Digit `tid`: counts per warp -> exclusive offsets over warps; publish the
-  // tile's count (inclusive for tile 0) before scanning, so successors can
-  // proceed as early as possible.
+  // Digit `tid`: counts per warp -> exclusive offsets over warps (kept in
+  // registers); publish the tile's count (inclusive for tile 0) before
+  // scanning, so successors can proceed as early as possible.
   uint32_t tile_cnt = 0, glob_cnt = 0, valid_cnt = 0;
+  uint32_t wexcl[NWARPS];
   if(tid < radix_bins) {
-#pragma unroll 4
+#pragma unroll
     for(int w = 0; w < NWARPS; ++w) {
-      uint32_t c = whist[w * radix_bins + tid];
-      whist[w * radix_bins + tid] = tile_cnt;
+      const uint32_t c = warp_count(w, tid);
+      wexcl[w] = tile_cnt;
       tile_cnt += c;
     }
     valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
@@ -395,8 +409,8 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   lookback_window_t<WINDOW> lbw;
   if(tid < radix_bins) {
     if(tile > 0) lbw.issue(t.lb_row + tid - radix_bins, tile);
-#pragma unroll 4
-    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] += tile_start;
+#pragma unroll
+    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] = wexcl[w] + tile_start;
   }
   __syncthreads();
 

@@ -487,7 +487,7 @@ scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_stat
   constexpr int TILE = NT * VT;
   constexpr int NW = NT / 32;
   static_assert(NW >= 2, "the copy thread is outside warp 0");
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
   __shared__ T warp_tot[NW];
   __shared__ T s_val[NW];

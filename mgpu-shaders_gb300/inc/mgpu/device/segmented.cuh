@@ -441,146 +441,262 @@ struct seg_status_t {
   }
 };
 
-template<typename T, typename op_t, int NT, int VT, bool exclusive>
-__global__ void __launch_bounds__(NT)
-seg_scan_kernel(const T* in, T* out, int64_t count, const int64_t* offsets, int64_t num_segments,
-  const int* tile_first, T init, op_t op, seg_status_t<T> st, uint32_t* tile_counter,
-  int* error) {
+// CTA-wide look-back over (head, value) pairs for seg_scan_defer_kernel: in
+// each round warp w reads the 32 predecessors base - (32 w + lane).  The walk
+// stops at an inclusive status or at a tile whose aggregate holds a head.
+// Every thread returns the same pair.
+template<int NW, typename T, typename op_t>
+__device__ seg_pair_t<T> seg_lookback_cta(const seg_status_t<T>& st, int64_t tile, op_t op,
+  int* error, T* s_v, uint32_t* s_f, int* s_info) {
   typedef seg_pair_t<T> P;
-  constexpr int TILE = NT * VT;
-  constexpr int NW = NT / 32;
-  __shared__ uint32_t heads[TILE / 32];
-  __shared__ T wv[NW];
-  __shared__ uint32_t wf[NW];
-  __shared__ T s_pv;
-  __shared__ uint32_t s_pf;
-  __shared__ int64_t s_tile;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if(tid == 0) s_tile = atomicAdd(tile_counter, 1u);
-  for(int i = tid; i < TILE / 32; i += NT) heads[i] = 0;
-  __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t base = tile * TILE;
-  const int valid = (int)min((int64_t)TILE, count - base);
-
-  // Mark the heads of the non-empty segments that start in this tile.
-  for(int64_t s = tile_first[tile] + tid; s < num_segments; s += NT) {
-    int64_t o = offsets[s];
-    if(o >= base + valid) break;
-    if(offsets[s + 1] > o && o >= base) {
-      int r = (int)(o - base);
-      atomicOr(&heads[r >> 5], 1u << (r & 31));
-    }
-  }
-  if(tile == 0 && tid == 0) atomicOr(&heads[0], 1u);
-  __syncthreads();
-
-  const int first = tid * VT;
-  T x[VT];
-  load_thread<T, VT>(in + base + first, valid - first, false, x, op_t::identity());
-  uint32_t hbits = 0;
-#pragma unroll
-  for(int i = 0; i < VT; ++i) {
-    int e = first + i;
-    hbits |= ((heads[e >> 5] >> (e & 31)) & 1u) << i;
-  }
-  // Inclusive pair scan inside the thread.
-  P acc { x[0], hbits & 1u };
-  T incv[VT];
-  incv[0] = x[0];
-#pragma unroll
-  for(int i = 1; i < VT; ++i) {
-    acc = seg_combine<T>(acc, P { x[i], (hbits >> i) & 1u }, op);
-    incv[i] = acc.v;
-  }
-  // Warp-inclusive scan of thread aggregates.
-  P w = acc;
-#pragma unroll
-  for(int off = 1; off < 32; off <<= 1) {
-    P y { __shfl_up_sync(0xffffffffu, w.v, off), __shfl_up_sync(0xffffffffu, w.f, off) };
-    if(lane >= off) w = seg_combine<T>(y, w, op);
-  }
-  P wex { __shfl_up_sync(0xffffffffu, w.v, 1), __shfl_up_sync(0xffffffffu, w.f, 1) };
-  if(lane == 31) { wv[warp] = w.v; wf[warp] = w.f; }
-  __syncthreads();
-  if(warp == 0) {
-    P t { op_t::identity(), 0u };
-    if(lane < NW) t = P { wv[lane], wf[lane] };
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  P acc { op_t::identity(), 0u };
+  bool have = false;
+  int64_t base = tile - 1;
+  for(int round = 0;; ++round) {
+    const int64_t j = base - (warp * 32 + lane);
+    P v { op_t::identity(), 0u };
+    uint32_t f = status_inclusive;
+    if(j >= 0) f = st.read(j, v);
+    const bool stop_here = f == status_inclusive || (f != status_invalid && v.f);
+    const uint32_t stop_mask = __ballot_sync(0xffffffffu, stop_here);
+    const int limit = stop_mask ? __ffs(stop_mask) - 1 : 31;
+    const bool missing = __any_sync(0xffffffffu, lane <= limit && f == status_invalid);
 #pragma unroll
     for(int off = 1; off < 32; off <<= 1) {
-      P y { __shfl_up_sync(0xffffffffu, t.v, off), __shfl_up_sync(0xffffffffu, t.f, off) };
-      if(lane >= off) t = seg_combine<T>(y, t, op);
+      P y { __shfl_down_sync(0xffffffffu, v.v, off), __shfl_down_sync(0xffffffffu, v.f, off) };
+      if(lane + off <= limit) v = seg_combine<T>(y, v, op);
     }
-    if(lane < NW) { wv[lane] = t.v; wf[lane] = t.f; }
+    if(lane == 0) {
+      int info = (stop_mask ? 1 : 0) | (missing ? 2 : 0);
+      if(warp == 0 && round &&
+         (round >= spin_limit || (0 == (round & (spin_poll_error - 1)) && error_raised(error))))
+        info |= 4;
+      s_v[warp] = v.v;
+      s_f[warp] = v.f;
+      s_info[warp] = info;
+    }
+    __syncthreads();
+    if(s_info[0] & 4) {
+      raise_error(error, err_lookback_timeout);
+      return acc;
+    }
+    bool miss = false;
+    int w_last = NW - 1, found = 0;
+#pragma unroll
+    for(int w = 0; w < NW; ++w) {
+      const int info = s_info[w];
+      if(!found && !miss) {
+        if(info & 2) miss = true;
+        else if(info & 1) { w_last = w; found = 1; }
+      }
+    }
+    P r { op_t::identity(), 0u };
+    if(!miss)
+      for(int w = w_last; w >= 0; --w) r = seg_combine<T>(r, P { s_v[w], s_f[w] }, op);
+    __syncthreads();
+    if(miss) {
+      __nanosleep(32);
+      continue;
+    }
+    acc = have ? seg_combine<T>(r, acc, op) : r;
+    have = true;
+    if(found) return acc;
+    base -= 32 * NW;
+  }
+}
+
+// Segmented scan with the deferred look-back of scan_defer_kernel: resident
+// CTAs loop over tiles; in one iteration a tile's values arrive by bulk copy,
+// its segment heads are marked and its (head, value) aggregate published; in
+// the next the CTA looks back, publishes the tile's inclusive pair, re-reads
+// the values from L2 and writes the scanned tile.  Elements are held in the
+// warp-striped layout of striped_t.
+template<typename T, int NT, int VT>
+struct seg_scan_defer_layout {
+  static constexpr size_t stage_bytes = sizeof(T) * NT * VT;
+  static constexpr size_t bar_off = stage_bytes;
+  static constexpr size_t bytes = bar_off + 16;
+};
+
+template<typename T, typename op_t, int NT, int VT, bool exclusive, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets,
+  int64_t num_segments, const int* tile_first, T init, op_t op, seg_status_t<T> st,
+  uint32_t* tile_counter, int* error, int vec_ok) {
+  typedef striped_t<T, VT> S;
+  typedef seg_pair_t<T> P;
+  typedef seg_scan_defer_layout<T, NT, VT> L;
+  constexpr int PER = S::PER, ROWS = S::ROWS;
+  constexpr int TILE = NT * VT;
+  constexpr int NW = NT / 32;
+  constexpr int HW = TILE / 32;
+  constexpr uint32_t PER_MASK = (1u << PER) - 1;
+  static_assert(NW >= 2, "the copy thread is outside warp 0");
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* bar = (uint64_t*)(smem + L::bar_off);
+  __shared__ uint32_t heads[2][HW];
+  __shared__ T wv[NW];
+  __shared__ uint32_t wf[NW];
+  __shared__ T s_v[NW];
+  __shared__ uint32_t s_f[NW];
+  __shared__ int s_info[NW];
+  __shared__ int64_t s_id;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t num_tiles = div_up(count, TILE);
+  const int64_t bulk_tiles = vec_ok ? count / TILE : 0;
+  const int copy_tid = NT - 32;
+
+  auto fetch = [&](int64_t id) {
+    s_id = id;
+    if(id < bulk_tiles) {
+      mbar_arrive_expect_tx(bar, (uint32_t)L::stage_bytes);
+      bulk_load(smem, in + id * TILE, (uint32_t)L::stage_bytes, bar);
+    }
+  };
+  // Head bits of this thread's PER elements of row r.
+  auto row_heads = [&](const uint32_t* h, int r) -> uint32_t {
+    const int e = S::offset(warp, lane, r);
+    return (h[e >> 5] >> (e & 31)) & PER_MASK;
+  };
+  if(tid == copy_tid) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    fetch(atomicAdd(tile_counter, 1u));
   }
   __syncthreads();
-  const P tile_agg { wv[NW - 1], wf[NW - 1] };
-  // Exclusive prefix of this thread within the tile (identity pair when none).
-  P tex { op_t::identity(), 0u };
-  if(lane) tex = wex;
-  if(warp) tex = seg_combine<T>(P { wv[warp - 1], wf[warp - 1] }, tex, op);
 
-  if(warp == 0) {
-    P prefix { op_t::identity(), 0u };
-    if(tile == 0) {
-      if(lane == 0) st.publish(0, status_inclusive, tile_agg);
-    } else {
-      if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
-      bool have = false;
-      int64_t b0 = tile - 1;
-      while(true) {
-        int64_t j = b0 - lane;
-        P v { op_t::identity(), 0u };
-        uint32_t flag = status_inclusive;
-        if(j >= 0) {
-          int spins = 0;
-          while(true) {
-            flag = st.read(j, v);
-            if(flag != status_invalid) break;
-            if(++spins >= spin_limit ||
-               (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
-              raise_error(error, err_lookback_timeout);
-              flag = status_inclusive;
-              v = P { op_t::identity(), 0u };
-              break;
-            }
-          }
+  int64_t prev = -1;
+  int hb = 0;                                  // heads buffer of `cur`
+  P prev_agg { op_t::identity(), 0u }, cur_agg { op_t::identity(), 0u };   // thread 0
+  uint32_t parity = 0;
+  while(true) {
+    int64_t next_id = 0;
+    if(tid == copy_tid) next_id = atomicAdd(tile_counter, 1u);
+    const int64_t cur = s_id;
+    const bool have_cur = cur < num_tiles;
+
+    if(have_cur) {
+      // Mark the heads of the non-empty segments that start in `cur`.
+      const int64_t base = cur * TILE;
+      const int valid = (int)min((int64_t)TILE, count - base);
+      uint32_t* h = heads[hb];
+      for(int i = tid; i < HW; i += NT) h[i] = 0;
+      __syncthreads();
+      for(int64_t sg = tile_first[cur] + tid; sg < num_segments; sg += NT) {
+        const int64_t o = offsets[sg];
+        if(o >= base + valid) break;
+        if(offsets[sg + 1] > o && o >= base) {
+          const int r = (int)(o - base);
+          atomicOr(&h[r >> 5], 1u << (r & 31));
         }
-        // Stop at an inclusive prefix or at any tile containing a head.
-        uint32_t stop = __ballot_sync(0xffffffffu, flag == status_inclusive || v.f);
-        int limit = stop ? __ffs(stop) - 1 : 31;
+      }
+      if(cur == 0 && tid == 0) atomicOr(&h[0], 1u);
+      __syncthreads();
+      // Ordered fold of the tile's pairs.
+      T x[VT];
+      if(cur < bulk_tiles) {
+        mbar_wait_bounded(bar, parity, error);   // a timeout raised the error
+        parity ^= 1;
+        const T* sx = (const T*)smem;
+#pragma unroll
+        for(int r = 0; r < ROWS; ++r) {
+          uint4 w = *reinterpret_cast<const uint4*>(sx + S::offset(warp, lane, r));
+          memcpy(&x[r * PER], &w, 16);
+        }
+      } else {
+        S::load(in + base, valid, false, warp, lane, x, op_t::identity());
+      }
+      P acc { op_t::identity(), 0u };
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        const uint32_t hr = row_heads(h, r);
+        P l { op_t::identity(), 0u };
+#pragma unroll
+        for(int j = 0; j < PER; ++j) l = seg_combine<T>(l, P { x[r * PER + j], (hr >> j) & 1u }, op);
 #pragma unroll
         for(int off = 1; off < 32; off <<= 1) {
-          P y { __shfl_down_sync(0xffffffffu, v.v, off), __shfl_down_sync(0xffffffffu, v.f, off) };
-          if(lane + off <= limit) v = seg_combine<T>(y, v, op);
+          P y { __shfl_down_sync(0xffffffffu, l.v, off), __shfl_down_sync(0xffffffffu, l.f, off) };
+          if(lane + off < 32) l = seg_combine<T>(l, y, op);
         }
-        P r { __shfl_sync(0xffffffffu, v.v, 0), __shfl_sync(0xffffffffu, v.f, 0) };
-        prefix = have ? seg_combine<T>(r, prefix, op) : r;
-        have = true;
-        if(stop) break;
-        b0 -= 32;
+        acc = seg_combine<T>(acc, P { __shfl_sync(0xffffffffu, l.v, 0),
+          __shfl_sync(0xffffffffu, l.f, 0) }, op);
       }
-      if(lane == 0) st.publish(tile, status_inclusive, seg_combine<T>(prefix, tile_agg, op));
+      if(lane == 0) { wv[warp] = acc.v; wf[warp] = acc.f; }
     }
-    if(lane == 0) { s_pv = prefix.v; s_pf = prefix.f; }
-  }
-  __syncthreads();
-  // Carry into the thread = prefix . tex; element i's inclusive pair is
-  // carry . (local pairs 0..i).  A head inside the thread cuts the carry.
-  const P carry = seg_combine<T>(P { s_pv, s_pf }, tex, op);
-  T y[VT];
-  bool seen_head = false;
+    __syncthreads();                           // stage consumed; warp totals visible
+    if(tid == copy_tid) fetch(next_id);
+    if(have_cur && tid == 0) {
+      P agg { op_t::identity(), 0u };
 #pragma unroll
-  for(int i = 0; i < VT; ++i) {
-    bool h = (hbits >> i) & 1u;
-    // Exclusive value before element i within its segment.
-    T before = (i == 0) ? carry.v : (seen_head ? incv[i - 1] : op(carry.v, incv[i - 1]));
-    seen_head |= h;
-    T incl = seen_head ? incv[i] : op(carry.v, incv[i]);
-    if(exclusive) y[i] = h ? init : op(init, before);
-    else y[i] = op(init, incl);
+      for(int w = 0; w < NW; ++w) agg = seg_combine<T>(agg, P { wv[w], wf[w] }, op);
+      st.publish(cur, cur == 0 ? status_inclusive : status_aggregate, agg);
+      cur_agg = agg;
+    }
+
+    if(prev >= 0) {
+      const int64_t base = prev * TILE;
+      const int valid = (int)min((int64_t)TILE, count - base);
+      const bool vec = vec_ok && valid == TILE;
+      const uint32_t* h = heads[hb ^ 1];
+      T x[VT];
+      S::load(in + base, valid, vec, warp, lane, x, op_t::identity());
+      P prefix { op_t::identity(), 0u };
+      if(prev > 0) {
+        prefix = seg_lookback_cta<NW, T>(st, prev, op, error, s_v, s_f, s_info);
+        if(tid == 0) st.publish(prev, status_inclusive, seg_combine<T>(prefix, prev_agg, op));
+      } else {
+        __syncthreads();
+      }
+      // Per row: the pair before this lane's first element, counted from the
+      // start of the warp's range.
+      P before[ROWS];
+      P acc { op_t::identity(), 0u };
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        const uint32_t hr = row_heads(h, r);
+        P l { op_t::identity(), 0u };
+#pragma unroll
+        for(int j = 0; j < PER; ++j) l = seg_combine<T>(l, P { x[r * PER + j], (hr >> j) & 1u }, op);
+        P inc = l;
+#pragma unroll
+        for(int off = 1; off < 32; off <<= 1) {
+          P y { __shfl_up_sync(0xffffffffu, inc.v, off), __shfl_up_sync(0xffffffffu, inc.f, off) };
+          if(lane >= off) inc = seg_combine<T>(y, inc, op);
+        }
+        P ex { __shfl_up_sync(0xffffffffu, inc.v, 1), __shfl_up_sync(0xffffffffu, inc.f, 1) };
+        if(lane == 0) ex = P { op_t::identity(), 0u };
+        before[r] = seg_combine<T>(acc, ex, op);
+        acc = seg_combine<T>(acc, P { __shfl_sync(0xffffffffu, inc.v, 31),
+          __shfl_sync(0xffffffffu, inc.f, 31) }, op);
+      }
+      if(lane == 0) { wv[warp] = acc.v; wf[warp] = acc.f; }
+      __syncthreads();
+      P carry = prefix;
+#pragma unroll
+      for(int w = 0; w < NW; ++w)
+        if(w < warp) carry = seg_combine<T>(carry, P { wv[w], wf[w] }, op);
+#pragma unroll
+      for(int r = 0; r < ROWS; ++r) {
+        const uint32_t hr = row_heads(h, r);
+        P run = seg_combine<T>(carry, before[r], op);
+#pragma unroll
+        for(int j = 0; j < PER; ++j) {
+          const uint32_t hd = (hr >> j) & 1u;
+          const T xv = x[r * PER + j];
+          if(exclusive) x[r * PER + j] = hd ? init : op(init, run.v);
+          run = seg_combine<T>(run, P { xv, hd }, op);
+          if(!exclusive) x[r * PER + j] = op(init, run.v);
+        }
+      }
+      S::store(out + base, valid, vec, warp, lane, x);
+    }
+    __syncthreads();
+    if(!have_cur) break;
+    prev = cur;
+    prev_agg = cur_agg;
+    hb ^= 1;
   }
-  store_thread<T, VT>(out + base + first, valid - first, false, y);
 }
 
 }  // namespace device

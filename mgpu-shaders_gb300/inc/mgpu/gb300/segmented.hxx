@@ -7,7 +7,8 @@
 //   sort: memset, classify, persistent small-segment sort, then for the
 //         segments larger than one tile a histogram launch and one onesweep
 //         pass per 8-bit digit over all of their tiles together;
-//   scan: memset, per-tile segment lookup, one single-pass look-back scan.
+//   scan: memset, per-tile segment lookup, one persistent look-back scan
+//         (seg_scan_defer_kernel).
 // No host synchronisation; graph-capturable.
 #pragma once
 
@@ -134,10 +135,12 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   T init = op_t::identity(), op_t op = op_t()) {
   using namespace device;
   constexpr int NT = 256;
-  constexpr int VT = sizeof(T) == 4 ? 16 : 8;
+  constexpr int VT = sizeof(T) == 4 ? 32 : 16;
+  constexpr int MINB = 3;
   constexpr int TILE = NT * VT;
   if(count < 0 || num_segments < 0 || num_segments > INT32_MAX) return MGPU_ERR_INVALID_ARG;
   const int64_t num_tiles = div_up(count, TILE);
+  if(num_tiles > 0x7fffffffll) return MGPU_ERR_INVALID_ARG;
   aux_layout_t lay;
   size_t cnt_off = lay.add(16);
   size_t flags_off = lay.add(sizeof(uint32_t) * num_tiles);
@@ -159,10 +162,16 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   if(st) return st;
   seg_status_t<T> status { (uint32_t*)(base + flags_off), (uint64_t*)(base + vals_off),
     num_tiles };
+  typedef seg_scan_defer_layout<T, NT, VT> SL;
+  auto k = seg_scan_defer_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, MINB>;
+  if(!ctx.allow_smem(k, SL::bytes)) return MGPU_ERR_CUDA;
+  const int per_sm = ctx.resident_ctas(k, NT, SL::bytes);
+  if(per_sm < 1) return MGPU_ERR_CUDA;
+  const int64_t grid = std::min<int64_t>((int64_t)per_sm * ctx.sm_count, num_tiles);
+  const int vec = aligned16_host(in) && aligned16_host(out);
   return ctx.launch("seg_scan", [&] {
-    seg_scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc>
-      <<<(unsigned)num_tiles, NT, 0, ctx.stream>>>(in, out, count, offsets, num_segments, first,
-        init, op, status, (uint32_t*)base, ctx.d_error);
+    k<<<(unsigned)grid, NT, SL::bytes, ctx.stream>>>(in, out, count, offsets, num_segments,
+      first, init, op, status, (uint32_t*)base, ctx.d_error, vec);
   });
 }
 
