@@ -101,27 +101,30 @@ __device__ __forceinline__ void scan_256_pair(uint32_t& x, uint32_t& y, uint32_t
   }
 }
 
-// Histogram of every digit place in one read.  Also clears the look-back
-// status words of all passes (zero_words uint4s), which must be zero before
-// the first scatter pass starts.
-template<typename K, int NT, int PASSES>
+// Histogram of every digit place in one read.  Each bin has LANES copies
+// and lane l updates copy l % LANES, so the 32 lanes of a warp hit 32 (or,
+// with 16 copies, at worst 2 x 16) different banks and the shared-memory
+// atomics do not conflict; the copies are summed before one global atomic
+// per bin and CTA.  Dynamic shared memory: PASSES * 256 * LANES counters.
+template<typename K, int NT, int PASSES, int LANES>
 __global__ void __launch_bounds__(NT)
-radix_histogram(const K* keys, int64_t count, uint32_t* hist, uint4* zero, int64_t zero_vec4,
-  int vectorised) {
+radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised) {
   typedef typename radix_key<K>::bits_t U;
-  __shared__ uint32_t sh[PASSES * radix_bins];
+  constexpr int BINS = PASSES * radix_bins;
+  extern __shared__ __align__(16) uint32_t sh[];
   const int tid = threadIdx.x;
-  for(int i = tid; i < PASSES * radix_bins; i += NT) sh[i] = 0;
+  for(int i = tid; i < BINS * LANES / 4; i += NT)
+    reinterpret_cast<uint4*>(sh)[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+  const int copy = tid % LANES;
   const int64_t gid = (int64_t)blockIdx.x * NT + tid;
   const int64_t stride = (int64_t)gridDim.x * NT;
-  for(int64_t i = gid; i < zero_vec4; i += stride) zero[i] = make_uint4(0, 0, 0, 0);
-  __syncthreads();
 
   auto count_key = [&](K key) {
     U u = radix_key<K>::to_bits(key);
 #pragma unroll
     for(int p = 0; p < PASSES; ++p)
-      atomicAdd(&sh[p * radix_bins + extract_digit(u, 8 * p, 8)], 1u);
+      atomicAdd(&sh[(p * radix_bins + extract_digit(u, 8 * p, 8)) * LANES + copy], 1u);
   };
   constexpr int per_vec = 16 / sizeof(K);
   int64_t num_vec = vectorised ? count / per_vec : 0;
@@ -134,8 +137,12 @@ radix_histogram(const K* keys, int64_t count, uint32_t* hist, uint4* zero, int64
   }
   for(int64_t i = num_vec * per_vec + gid; i < count; i += stride) count_key(keys[i]);
   __syncthreads();
-  for(int i = tid; i < PASSES * radix_bins; i += NT)
-    if(sh[i]) atomicAdd(&hist[i], sh[i]);
+  for(int i = tid; i < BINS; i += NT) {
+    uint32_t sum = 0;
+#pragma unroll 8
+    for(int j = 0; j < LANES; ++j) sum += sh[i * LANES + ((i + j) & (LANES - 1))];
+    if(sum) atomicAdd(&hist[i], sum);
+  }
 }
 
 // Where one tile of a sort sits.  A plain sort is one sequence; a segmented

@@ -83,15 +83,19 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
 
   if(ctx.check(cudaMemsetAsync(base, 0, header_bytes, ctx.stream))) return MGPU_ERR_CUDA;
 
-  // Histogram of every digit place; also clears the look-back words.
+  // Histogram of every digit place: one CTA of 1024 threads per SM, the
+  // bins spread over 32 (4-byte keys) or 16 (8-byte keys) shared copies.
   {
-    constexpr int hnt = 512;
+    constexpr int hnt = 1024;
+    constexpr int lanes = passes <= 4 ? 32 : 16;
+    constexpr size_t hsmem = sizeof(uint32_t) * passes * radix_bins * lanes;
+    auto hk = radix_histogram<K, hnt, passes, lanes>;
+    if(!ctx.allow_smem(hk, hsmem)) return MGPU_ERR_CUDA;
     int64_t want = div_up(count, (int64_t)hnt * 16);
-    int grid = (int)std::min<int64_t>(std::max<int64_t>(want, 1), (int64_t)ctx.sm_count * 4);
+    int grid = (int)std::min<int64_t>(std::max<int64_t>(want, 1), (int64_t)ctx.sm_count);
     int vec = aligned16_host(keys);
     st = ctx.launch("radix_histogram", [&] {
-      radix_histogram<K, hnt, passes><<<grid, hnt, 0, ctx.stream>>>(keys, count, hist,
-        (uint4*)lookback, 0, vec);
+      hk<<<grid, hnt, hsmem, ctx.stream>>>(keys, count, hist, vec);
     });
     if(st) return st;
   }
