@@ -52,30 +52,79 @@ __device__ __forceinline__ idx_t merge_path(const K* a, idx_t a_count, const K* 
   return begin;
 }
 
-// Partitions of a two-array merge: mp[i] for diagonal min(i * spacing, total).
+// merge_path by a whole warp: each round the 32 lanes test the last position
+// of 32 equal chunks of the candidate range and keep the first chunk whose
+// test holds, so a range of n candidates takes about log32(n) rounds of
+// independent loads instead of log2(n) dependent ones.  Every lane returns
+// the result.
 template<typename K, typename comp_t>
+__device__ __forceinline__ int64_t merge_path_warp(const K* a, int64_t a_count, const K* b,
+  int64_t b_count, int64_t diag, comp_t comp) {
+  const int lane = threadIdx.x & 31;
+  int64_t begin = diag > b_count ? diag - b_count : 0;
+  int64_t end = diag < a_count ? diag : a_count;
+  while(end - begin > 32) {
+    // Chunk k is [begin + k step, begin + (k + 1) step) clipped to `end`;
+    // its last position is tested.
+    const int64_t step = (end - begin + 31) >> 5;
+    const int64_t start = begin + lane * step;
+    const int64_t probe = min(start + step, end) - 1;
+    const bool hit = start < end && comp(b[diag - 1 - probe], a[probe]);
+    const uint32_t mask = __ballot_sync(0xffffffffu, hit);
+    if(!mask) return end;
+    const int k = __ffs(mask) - 1;
+    const int64_t lo = begin + k * step;
+    end = min(end, lo + step);
+    begin = lo;
+  }
+  const int64_t probe = begin + lane;
+  const bool hit = probe < end && comp(b[diag - 1 - probe], a[probe]);
+  const uint32_t mask = __ballot_sync(0xffffffffu, hit);
+  return mask ? begin + __ffs(mask) - 1 : end;
+}
+
+// Partitions of a two-array merge: mp[i] for diagonal min(i * spacing,
+// total).  WARP: one warp per partition (few partitions: the search latency
+// dominates); otherwise one thread per partition (many partitions: the
+// kernel is bound by its loads).
+template<typename K, typename comp_t, bool WARP>
 __global__ void merge_partition_kernel(const K* a, int64_t a_count, const K* b, int64_t b_count,
   int64_t spacing, int64_t num_partitions, int64_t* mp, comp_t comp) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = WARP ? t >> 5 : t;
   if(i >= num_partitions) return;
-  int64_t diag = min(i * spacing, a_count + b_count);
-  mp[i] = merge_path(a, a_count, b, b_count, diag, comp);
+  const int64_t diag = min(i * spacing, a_count + b_count);
+  if(WARP) {
+    const int64_t r = merge_path_warp(a, a_count, b, b_count, diag, comp);
+    if((threadIdx.x & 31) == 0) mp[i] = r;
+  } else {
+    mp[i] = merge_path(a, a_count, b, b_count, diag, comp);
+  }
 }
 
 // Partitions of one mergesort pass over runs of `run` items: one per output
-// tile start.
-template<typename K, typename comp_t>
+// tile start (WARP as for merge_partition_kernel).
+template<typename K, typename comp_t, bool WARP>
 __global__ void mergesort_partition_kernel(const K* keys, int64_t count, int64_t run,
   int64_t spacing, int64_t num_partitions, int64_t* mp, comp_t comp) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = WARP ? t >> 5 : t;
   if(i >= num_partitions) return;
-  int64_t pos = min(i * spacing, count);
-  int64_t pair = pos / (2 * run);
-  int64_t a0 = pair * 2 * run;
-  int64_t a1 = min(a0 + run, count);
-  int64_t b1 = min(a0 + 2 * run, count);
-  mp[i] = merge_path(keys + a0, a1 - a0, keys + a1, b1 - a1, pos - a0, comp);
+  const int64_t pos = min(i * spacing, count);
+  const int64_t pair = pos / (2 * run);
+  const int64_t a0 = pair * 2 * run;
+  const int64_t a1 = min(a0 + run, count);
+  const int64_t b1 = min(a0 + 2 * run, count);
+  if(WARP) {
+    const int64_t r = merge_path_warp(keys + a0, a1 - a0, keys + a1, b1 - a1, pos - a0, comp);
+    if((threadIdx.x & 31) == 0) mp[i] = r;
+  } else {
+    mp[i] = merge_path(keys + a0, a1 - a0, keys + a1, b1 - a1, pos - a0, comp);
+  }
 }
+
+// Partition counts up to this use the warp search.
+constexpr int64_t warp_partition_limit = 8192;
 
 // Shared-memory plan of one merge tile: keys and values of the A and B
 // ranges, each placed so that its 16-byte-aligned global window starts on a

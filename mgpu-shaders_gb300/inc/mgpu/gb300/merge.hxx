@@ -51,8 +51,12 @@ status_t merge_kv(void* aux_data, size_t* aux_size, context_t& ctx,
     return MGPU_ERR_INVALID_ARG;
   int64_t* mp = (int64_t*)(base + mp_off);
   st = ctx.launch("merge_partition", [&] {
-    merge_partition_kernel<K, comp_t><<<(unsigned)div_up(num_partitions, 256), 256, 0,
-      ctx.stream>>>(a_keys, a_count, b_keys, b_count, NV, num_partitions, mp, comp);
+    if(num_partitions <= warp_partition_limit)
+      merge_partition_kernel<K, comp_t, true><<<(unsigned)div_up(num_partitions, 8), 256, 0,
+        ctx.stream>>>(a_keys, a_count, b_keys, b_count, NV, num_partitions, mp, comp);
+    else
+      merge_partition_kernel<K, comp_t, false><<<(unsigned)div_up(num_partitions, 256), 256, 0,
+        ctx.stream>>>(a_keys, a_count, b_keys, b_count, NV, num_partitions, mp, comp);
   });
   if(st) return st;
   auto kernel = merge_kernel<K, V, NT, VT, comp_t>;
@@ -137,8 +141,12 @@ status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys,
   for(int pass = 0; pass < num_passes; ++pass) {
     int64_t run = (int64_t)NV << pass;
     st = ctx.launch("mergesort_partition", [&] {
-      mergesort_partition_kernel<K, comp_t><<<(unsigned)div_up(num_tiles + 1, 256), 256, 0,
-        ctx.stream>>>(kin, count, run, NV, num_tiles + 1, mp, comp);
+      if(num_tiles + 1 <= warp_partition_limit)
+        mergesort_partition_kernel<K, comp_t, true><<<(unsigned)div_up(num_tiles + 1, 8), 256, 0,
+          ctx.stream>>>(kin, count, run, NV, num_tiles + 1, mp, comp);
+      else
+        mergesort_partition_kernel<K, comp_t, false><<<(unsigned)div_up(num_tiles + 1, 256), 256,
+          0, ctx.stream>>>(kin, count, run, NV, num_tiles + 1, mp, comp);
     });
     if(st) return st;
     int bulk = aligned16_host(kin) && (!has_values || aligned16_host(vin));
