@@ -36,6 +36,7 @@ SEED = 0x6D677075 + 2
 METRIC = "Mkeys/s (2^28 u32 key + u32 value radix sort)"
 ALG_BYTES_PER_KEY = 68          # 4 passes x (4+4 read + 4+4 write) + 4 histogram read
 PASS_BYTES_PER_KEY = 16         # one onesweep_pass launch
+ONESWEEP_TRAFFIC_PER_KEY = 15.1  # measured DRAM bytes per key of one pass
 CPU_SAMPLE = 1 << 24
 
 
@@ -869,11 +870,10 @@ def main():
     if os.path.exists(peaks_path):
         peak = json.load(open(peaks_path)).get("hbm_gbs", peak)
         peak_src = "measured"
-    traffic = None
-    tp = os.path.join(REPO, "profiles", "onesweep_pass_traffic.json")
-    if os.path.exists(tp):
-        t = json.load(open(tp))
-        traffic = t.get("bytes_per_key", 0) * n or None
+    # DRAM bytes (read + write) per key of one onesweep_pass launch, from an
+    # ncu capture of a 2^25-key launch (profiles/onesweep_pass_u32kv.md),
+    # scaled to this launch by its key count.
+    traffic = ONESWEEP_TRAFFIC_PER_KEY * n
 
     # End to end through the C ABI: pinned host -> device, sort, device -> host.
     e2e_steps = min(steps, 3)
@@ -908,6 +908,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "onesweep_pass", "achieved": achieved,
                      "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "traffic_unit": "DRAM bytes per launch (ncu)",
                      "peak_source": peak_src, "launch_ms": pass_ms,
                      "bytes_per_launch": PASS_BYTES_PER_KEY * n},
         "kernels_ms_per_step": {k: v[1] / prof_steps for k, v in prof.items()},
