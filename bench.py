@@ -8,7 +8,9 @@ One step = one in-place radix sort of 2^28 key/value pairs through the C ABI
 (outside the step's CUDA event pair); the input is 2 GiB (> L2), so no L2
 flush is needed.  `value` is device throughput (Mkeys/s from the mean of the
 per-step event times); `e2e` is the same metric through the C ABI with the
-keys/values starting and ending in pinned host memory.
+keys/values starting and ending in pinned host memory (uploads, sorts and
+downloads on three streams over two buffer sets, so neighbouring steps'
+copies overlap each sort).
 `roofline` covers the dominant kernel (onesweep_pass): 16 algorithmic bytes
 per key per launch, divided by its mean event-timed duration.
 
@@ -875,28 +877,54 @@ def main():
     # scaled to this launch by its key count.
     traffic = ONESWEEP_TRAFFIC_PER_KEY * n
 
-    # End to end through the C ABI: pinned host -> device, sort, device -> host.
-    e2e_steps = min(steps, 3)
+    # End to end through the C ABI: every step copies its keys and values from
+    # pinned host memory, sorts them and copies the result back, as a caller
+    # streaming sorts would pipeline them: uploads, sorts and downloads run on
+    # three streams (one context each) over two device buffer sets, so step
+    # i + 1's upload and step i - 1's download overlap step i's sort.
+    e2e_steps = max(4, min(steps, 6))
     hk = torch.from_numpy(keys_h).pin_memory()
     hv = torch.from_numpy(vals_h).pin_memory()
-    ok_k = torch.empty_like(hk).pin_memory()
-    ok_v = torch.empty_like(hv).pin_memory()
-    dk, dv = copies[0]
+    outs = [(torch.empty_like(hk).pin_memory(), torch.empty_like(hv).pin_memory())
+            for _ in range(2)]
     lib = mg.lib()
     nbytes = 4 * n
+    streams = [torch.cuda.Stream() for _ in range(3)]          # upload, sort, download
+    up, srt, down = [mg.Context(local, stream=st_.cuda_stream) for st_ in streams]
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(e2e_steps):
-        ctx._check(lib.mgpu_memcpy(ctx.handle, dk.ptr, hk.data_ptr(), nbytes))
-        ctx._check(lib.mgpu_memcpy(ctx.handle, dv.ptr, hv.data_ptr(), nbytes))
-        ctx.radix_sort(dk, dv, aux=aux)
-        ctx._check(lib.mgpu_memcpy(ctx.handle, ok_k.data_ptr(), dk.ptr, nbytes))
-        ctx._check(lib.mgpu_memcpy(ctx.handle, ok_v.data_ptr(), dv.ptr, nbytes))
+    for st_ in streams:
+        st_.wait_event(e0)
+    freed = [None, None]         # download of the buffer set's previous step done
+    for i in range(e2e_steps):
+        b = i % 2
+        dk, dv = copies[b]
+        if freed[b] is not None:
+            streams[0].wait_event(freed[b])
+        up._check(lib.mgpu_memcpy(up.handle, dk.ptr, hk.data_ptr(), nbytes))
+        up._check(lib.mgpu_memcpy(up.handle, dv.ptr, hv.data_ptr(), nbytes))
+        uploaded = torch.cuda.Event()
+        uploaded.record(streams[0])
+        streams[1].wait_event(uploaded)
+        srt.radix_sort(dk, dv, aux=aux)
+        sorted_ = torch.cuda.Event()
+        sorted_.record(streams[1])
+        streams[2].wait_event(sorted_)
+        down._check(lib.mgpu_memcpy(down.handle, outs[b][0].data_ptr(), dk.ptr, nbytes))
+        down._check(lib.mgpu_memcpy(down.handle, outs[b][1].data_ptr(), dv.ptr, nbytes))
+        freed[b] = torch.cuda.Event()
+        freed[b].record(streams[2])
+    for st_ in streams:
+        done = torch.cuda.Event()
+        done.record(st_)
+        stream.wait_event(done)
     e1.record(stream)
     torch.cuda.synchronize()
+    for c_ in (up, srt, down):
+        c_.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    e2e_ok = bool(np.array_equal(keys_h[ok_v.numpy()], ok_k.numpy()))
+    e2e_ok = all(bool(np.array_equal(keys_h[ov.numpy()], ok.numpy())) for ok, ov in outs)
 
     value = n * world / (ms * 1e-3) / 1e6
     line = {
@@ -914,6 +942,7 @@ def main():
         "kernels_ms_per_step": {k: v[1] / prof_steps for k, v in prof.items()},
         "e2e": {"value": n * world / (e2e_ms * 1e-3) / 1e6, "unit": "Mkeys/s",
                 "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                "steps": e2e_steps, "streams": 3,
                 "ms_per_step": e2e_ms},
         "clocks": clk,
         "checks": {"timed_output_sorted_stable": ok_sorted, "e2e_output": e2e_ok},
