@@ -17,6 +17,11 @@ mgpu_status_t run(mgpu_context* c, const void* ak, const void* av, int64_t an, c
   if(variant == 1)
     return merge_kv<NT1, 8>(aux, aux_size, c->ctx, (const K*)ak, (const V*)av, an, (const K*)bk,
       (const V*)bv, bn, (K*)ck, (V*)cv, comp_t());
+  // The even shape (stride-16 or -8 shared-memory accesses per thread).
+  constexpr int VT_EVEN = sizeof(K) == 4 ? 16 : 8;
+  if(variant == 2)
+    return merge_kv<256, VT_EVEN>(aux, aux_size, c->ctx, (const K*)ak, (const V*)av, an,
+      (const K*)bk, (const V*)bv, bn, (K*)ck, (V*)cv, comp_t());
   return merge_kv(aux, aux_size, c->ctx, (const K*)ak, (const V*)av, an, (const K*)bk,
     (const V*)bv, bn, (K*)ck, (V*)cv, comp_t());
 }

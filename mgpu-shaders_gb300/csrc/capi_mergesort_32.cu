@@ -21,6 +21,14 @@ mgpu_status_t mergesort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys, 
         return mergesort_kv<NT1, 8, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           greater_t<K>());
       }
+      constexpr int VT_EVEN = sizeof(K) == 4 ? 16 : 8;
+      if(variant == 2) {
+        if(comp == MGPU_LESS)
+          return mergesort_kv<256, VT_EVEN, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+            less_t<K>());
+        return mergesort_kv<256, VT_EVEN, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+          greater_t<K>());
+      }
       if(comp == MGPU_LESS)
         return mergesort_kv<0, 0, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           less_t<K>());

@@ -25,11 +25,12 @@ inline const char* scan_name(int bytes, int v) {
   return bytes == 4 ? n4[v] : n8[v];
 }
 
-// merge / mergesort: 4-byte keys {256x16, 256x8}; 8-byte keys {256x8, 128x8}.
-inline int merge_count(int) { return 2; }
+// merge / mergesort: 4-byte keys {256x15, 256x8, 256x16}; 8-byte keys
+// {256x7, 128x8, 256x8} (odd shapes keep shared-memory strides odd).
+inline int merge_count(int) { return 3; }
 inline const char* merge_name(int bytes, int v) {
-  static const char* n4[] = { "256x16", "256x8" };
-  static const char* n8[] = { "256x8", "128x8" };
+  static const char* n4[] = { "256x15", "256x8", "256x16" };
+  static const char* n8[] = { "256x7", "128x8", "256x8" };
   return bytes == 4 ? n4[v] : n8[v];
 }
 

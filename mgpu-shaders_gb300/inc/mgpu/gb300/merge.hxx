@@ -22,8 +22,10 @@ template<typename T> using less_t = device::less_t<T>;
 template<typename T> using greater_t = device::greater_t<T>;
 
 template<int key_bytes> struct merge_tuning;
-template<> struct merge_tuning<4> { enum { nt = 256, vt = 16 }; };
-template<> struct merge_tuning<8> { enum { nt = 256, vt = 8 }; };
+// Odd items per thread keep the per-thread strides of the serial merge and of
+// the output staging odd in shared memory, so they do not collide on banks.
+template<> struct merge_tuning<4> { enum { nt = 256, vt = 15 }; };
+template<> struct merge_tuning<8> { enum { nt = 256, vt = 7 }; };
 
 template<int nt = 0, int vt = 0, typename K, typename V, typename comp_t>
 status_t merge_kv(void* aux_data, size_t* aux_size, context_t& ctx,
