@@ -123,7 +123,8 @@ __global__ void mergesort_partition_kernel(const K* keys, int64_t count, int64_t
   }
 }
 
-// Partition counts up to this use the warp search.
+// Partition counts up to this use the warp search (inside the mergesort pass
+// kernel itself, so such passes need no partition launch).
 constexpr int64_t warp_partition_limit = 8192;
 
 // Shared-memory plan of one merge tile: keys and values of the A and B
@@ -328,8 +329,24 @@ mergesort_pass_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_o
   const int64_t b1 = min(a0 + 2 * run, count);
   const int64_t diag0 = pos0 - a0;
   const int64_t diag1 = min(diag0 + NV, b1 - a0);
-  const int64_t mp0 = mp[tile];
-  const int64_t mp1 = diag1 == b1 - a0 ? a1 - a0 : mp[tile + 1];
+  int64_t mp0, mp1;
+  if(mp) {
+    mp0 = mp[tile];
+    mp1 = diag1 == b1 - a0 ? a1 - a0 : mp[tile + 1];
+  } else {
+    // No partition launch: warps 0 and 1 search this tile's two splits.
+    __shared__ int64_t s_mp[2];
+    const int warp = threadIdx.x >> 5;
+    if(warp < 2) {
+      const int64_t d = warp ? diag1 : diag0;
+      const int64_t r = (warp && d == b1 - a0) ? a1 - a0 :
+        merge_path_warp(keys_in + a0, a1 - a0, keys_in + a1, b1 - a1, d, comp);
+      if((threadIdx.x & 31) == 0) s_mp[warp] = r;
+    }
+    __syncthreads();
+    mp0 = s_mp[0];
+    mp1 = s_mp[1];
+  }
   merge_tile_t<K, V, NT, VT, comp_t>::run(smem, keys_in, vals_in, count, a0 + mp0, a0 + mp1,
     keys_in, vals_in, count, a1 + diag0 - mp0, a1 + diag1 - mp1, keys_out, vals_out, pos0,
     bulk_ok != 0, comp, error);

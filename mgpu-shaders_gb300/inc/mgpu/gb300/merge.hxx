@@ -142,19 +142,18 @@ status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys,
   if(!ctx.allow_smem(kernel, L::bytes)) return MGPU_ERR_CUDA;
   for(int pass = 0; pass < num_passes; ++pass) {
     int64_t run = (int64_t)NV << pass;
-    st = ctx.launch("mergesort_partition", [&] {
-      if(num_tiles + 1 <= warp_partition_limit)
-        mergesort_partition_kernel<K, comp_t, true><<<(unsigned)div_up(num_tiles + 1, 8), 256, 0,
-          ctx.stream>>>(kin, count, run, NV, num_tiles + 1, mp, comp);
-      else
+    const bool fused = num_tiles + 1 <= warp_partition_limit;
+    if(!fused) {
+      st = ctx.launch("mergesort_partition", [&] {
         mergesort_partition_kernel<K, comp_t, false><<<(unsigned)div_up(num_tiles + 1, 256), 256,
           0, ctx.stream>>>(kin, count, run, NV, num_tiles + 1, mp, comp);
-    });
-    if(st) return st;
+      });
+      if(st) return st;
+    }
     int bulk = aligned16_host(kin) && (!has_values || aligned16_host(vin));
     st = ctx.launch("mergesort_pass", [&] {
       kernel<<<(unsigned)num_tiles, NT, L::bytes, ctx.stream>>>(kin, vin, kout, vout, count, run,
-        mp, bulk, comp, ctx.d_error);
+        fused ? nullptr : mp, bulk, comp, ctx.d_error);
     });
     if(st) return st;
     std::swap(kin, kout);
