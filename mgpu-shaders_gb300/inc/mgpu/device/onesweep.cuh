@@ -294,6 +294,17 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     if(HAS_V) bulk_load(vs, a.vals_in + base, vbytes, bar);
   }
 
+  // Concentration of this pass's digits: when some digit holds more than
+  // 1/128 of the keys, rows of 32 equal digits become likely (equal keys sit
+  // together after earlier passes) and the ranking checks for them.  Warp
+  // maxima and sums of the digit totals go to scan scratch words 16..31.
+  if(tid < radix_bins) {
+    const uint32_t h = t.hist[tid];
+    const uint32_t m = __reduce_max_sync(0xffffffffu, h);
+    const uint32_t sum = __reduce_add_sync(0xffffffffu, h);
+    if(lane == 0) { stmp[16 + warp] = m; stmp[24 + warp] = sum; }
+  }
+
   // Element e of item i in this thread: warp-contiguous rows of 32 lanes,
   // e = warp_base + 32 * i + lane; it is in range while 32 * i < rem.
   const int warp_base = warp * 32 * ITEMS;
@@ -315,9 +326,17 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) k[i] = ks[warp_base + 32 * i + lane];
   } else {
+    __syncthreads();
     const U* src = a.keys_in + base + warp_base + lane;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) k[i] = 32 * i < rem ? src[32 * i] : ~(U)0;
+  }
+  bool check_uniform;
+  {
+    uint32_t mx = 0, total = 0;
+#pragma unroll
+    for(int w = 0; w < radix_bins / 32; ++w) { mx = max(mx, stmp[16 + w]); total += stmp[24 + w]; }
+    check_uniform = (uint64_t)mx * 128 > total;
   }
   if(a.first) {
 #pragma unroll
@@ -360,6 +379,17 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     for(int i = 0; i < ITEMS; ++i) {
       const uint32_t d = extract_digit(k[i], a.shift, 8);
       const uint32_t hi = (d >> 4) & 1;            // mask in the upper half
+      if(check_uniform && __all_sync(0xffffffffu, d == __shfl_sync(0xffffffffu, d, 0))) {
+        // One digit across the row (common once equal keys sit together):
+        // the peers are the whole warp, and same-address atomics are skipped.
+        uint32_t* cw = &mw[2 * d + 1 - hi];
+        const uint32_t cnt = *cw;
+        __syncwarp();
+        if(lane == 0) *cw = cnt + 32;
+        __syncwarp();
+        r[i] = cnt + lane;
+        continue;
+      }
       atomicOr(&mw[2 * d + hi], lane_bit);
       __syncwarp();
       const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
