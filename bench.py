@@ -891,39 +891,47 @@ def main():
     nbytes = 4 * n
     streams = [torch.cuda.Stream() for _ in range(3)]          # upload, sort, download
     up, srt, down = [mg.Context(local, stream=st_.cuda_stream) for st_ in streams]
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for st_ in streams:
-        st_.wait_event(e0)
-    freed = [None, None]         # download of the buffer set's previous step done
-    for i in range(e2e_steps):
-        b = i % 2
-        dk, dv = copies[b]
-        if freed[b] is not None:
-            streams[0].wait_event(freed[b])
-        up._check(lib.mgpu_memcpy(up.handle, dk.ptr, hk.data_ptr(), nbytes))
-        up._check(lib.mgpu_memcpy(up.handle, dv.ptr, hv.data_ptr(), nbytes))
-        uploaded = torch.cuda.Event()
-        uploaded.record(streams[0])
-        streams[1].wait_event(uploaded)
-        srt.radix_sort(dk, dv, aux=aux)
-        sorted_ = torch.cuda.Event()
-        sorted_.record(streams[1])
-        streams[2].wait_event(sorted_)
-        down._check(lib.mgpu_memcpy(down.handle, outs[b][0].data_ptr(), dk.ptr, nbytes))
-        down._check(lib.mgpu_memcpy(down.handle, outs[b][1].data_ptr(), dv.ptr, nbytes))
-        freed[b] = torch.cuda.Event()
-        freed[b].record(streams[2])
-    for st_ in streams:
-        done = torch.cuda.Event()
-        done.record(st_)
-        stream.wait_event(done)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    for c_ in (up, srt, down):
-        c_.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+
+    def e2e_run(num_steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for st_ in streams:
+            st_.wait_event(e0)
+        freed = [None, None]     # download of the buffer set's previous step done
+        for i in range(num_steps):
+            b = i % 2
+            dk, dv = copies[b]
+            if freed[b] is not None:
+                streams[0].wait_event(freed[b])
+            up._check(lib.mgpu_memcpy(up.handle, dk.ptr, hk.data_ptr(), nbytes))
+            up._check(lib.mgpu_memcpy(up.handle, dv.ptr, hv.data_ptr(), nbytes))
+            uploaded = torch.cuda.Event()
+            uploaded.record(streams[0])
+            streams[1].wait_event(uploaded)
+            srt.radix_sort(dk, dv, aux=aux)
+            sorted_ = torch.cuda.Event()
+            sorted_.record(streams[1])
+            streams[2].wait_event(sorted_)
+            down._check(lib.mgpu_memcpy(down.handle, outs[b][0].data_ptr(), dk.ptr, nbytes))
+            down._check(lib.mgpu_memcpy(down.handle, outs[b][1].data_ptr(), dv.ptr, nbytes))
+            freed[b] = torch.cuda.Event()
+            freed[b].record(streams[2])
+        for st_ in streams:
+            done = torch.cuda.Event()
+            done.record(st_)
+            stream.wait_event(done)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        for c_ in (up, srt, down):
+            c_.synchronize()
+        return e0.elapsed_time(e1)
+
+    e2e_run(2)                   # untimed warm-up of the copy path and the streams
+    # Host<->device bandwidth on this machine is shared with other tenants'
+    # jobs: take the median of three timed runs.
+    e2e_runs = [e2e_run(e2e_steps) / e2e_steps for _ in range(3)]
+    e2e_ms = statistics.median(e2e_runs)
     e2e_ok = all(bool(np.array_equal(keys_h[ov.numpy()], ok.numpy())) for ok, ov in outs)
 
     value = n * world / (ms * 1e-3) / 1e6
@@ -942,7 +950,7 @@ def main():
         "kernels_ms_per_step": {k: v[1] / prof_steps for k, v in prof.items()},
         "e2e": {"value": n * world / (e2e_ms * 1e-3) / 1e6, "unit": "Mkeys/s",
                 "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
-                "steps": e2e_steps, "streams": 3,
+                "steps": e2e_steps, "streams": 3, "runs_ms_per_step": e2e_runs,
                 "ms_per_step": e2e_ms},
         "clocks": clk,
         "checks": {"timed_output_sorted_stable": ok_sorted, "e2e_output": e2e_ok},
