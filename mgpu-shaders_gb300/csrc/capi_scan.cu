@@ -7,14 +7,14 @@ using namespace mgpu::gb300;
 
 namespace {
 
-template<int NT, int VT, int STAGES, int LBK, int MINB, typename T, typename op_t>
+template<int NT, int VT, int PERSISTENT, int MINB, typename T, typename op_t>
 mgpu_status_t scan_shape(mgpu_context* c, mgpu_scan_type_t st, const T* in, T* out,
   int64_t count, T init, T* reduction, void* aux, size_t* aux_size) {
   if(st == MGPU_SCAN_EXC)
-    return scan<scan_type_exc, NT, VT, STAGES, LBK, MINB>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
+    return scan<scan_type_exc, NT, VT, PERSISTENT, MINB>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
       reduction);
   if(st == MGPU_SCAN_INC)
-    return scan<scan_type_inc, NT, VT, STAGES, LBK, MINB>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
+    return scan<scan_type_inc, NT, VT, PERSISTENT, MINB>(aux, aux_size, c->ctx, in, count, out, init, op_t(),
       reduction);
   return MGPU_ERR_INVALID_ARG;
 }
@@ -28,21 +28,21 @@ mgpu_status_t run_scan(mgpu_context* c, mgpu_scan_type_t st, const void* in, voi
   const T* i = (const T*)in;
   T* o = (T*)out;
   T* r = (T*)reduction;
-#define MGPU_SCAN_SHAPE(nt, vt, stages, lbk, minb) \
-  scan_shape<nt, vt, stages, lbk, minb, T, op_t>(c, st, i, o, count, init, r, aux, aux_size)
+#define MGPU_SCAN_SHAPE(nt, vt, persistent, minb) \
+  scan_shape<nt, vt, persistent, minb, T, op_t>(c, st, i, o, count, init, r, aux, aux_size)
   if constexpr(sizeof(T) == 4) {
     switch(variant) {
-      case 1: return MGPU_SCAN_SHAPE(512, 32, 1, 0, 2);
-      case 2: return MGPU_SCAN_SHAPE(256, 16, 1, 0, 6);
-      case 3: return MGPU_SCAN_SHAPE(256, 32, 0, 1, 4);
-      default: return MGPU_SCAN_SHAPE(256, 32, 1, 0, 4);
+      case 1: return MGPU_SCAN_SHAPE(512, 32, 1, 2);
+      case 2: return MGPU_SCAN_SHAPE(256, 16, 1, 6);
+      case 3: return MGPU_SCAN_SHAPE(256, 32, 0, 4);
+      default: return MGPU_SCAN_SHAPE(256, 32, 1, 4);
     }
   } else {
     switch(variant) {
-      case 1: return MGPU_SCAN_SHAPE(256, 16, 1, 0, 4);
-      case 2: return MGPU_SCAN_SHAPE(256, 8, 1, 0, 6);
-      case 3: return MGPU_SCAN_SHAPE(256, 16, 0, 1, 4);
-      default: return MGPU_SCAN_SHAPE(512, 16, 1, 0, 2);
+      case 1: return MGPU_SCAN_SHAPE(256, 16, 1, 4);
+      case 2: return MGPU_SCAN_SHAPE(256, 8, 1, 6);
+      case 3: return MGPU_SCAN_SHAPE(256, 16, 0, 4);
+      default: return MGPU_SCAN_SHAPE(512, 16, 1, 2);
     }
   }
 #undef MGPU_SCAN_SHAPE

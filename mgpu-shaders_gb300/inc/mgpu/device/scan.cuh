@@ -261,41 +261,6 @@ __device__ __forceinline__ T warp_reduce(T x, op_t op) {
   return x;
 }
 
-// Loads VT consecutive elements of thread `tid` (thread-contiguous layout),
-// with 16-byte vector loads when the whole tile is in range and aligned.
-template<typename T, int VT>
-__device__ __forceinline__ void load_thread(const T* src, int valid_here, bool vec, T (&x)[VT],
-  T fill) {
-  if(vec) {
-    constexpr int per = 16 / sizeof(T);
-    static_assert(VT % per == 0, "vector width");
-#pragma unroll
-    for(int q = 0; q < VT / per; ++q) {
-      uint4 w = reinterpret_cast<const uint4*>(src)[q];
-      memcpy(&x[q * per], &w, 16);
-    }
-  } else {
-#pragma unroll
-    for(int i = 0; i < VT; ++i) x[i] = i < valid_here ? src[i] : fill;
-  }
-}
-
-template<typename T, int VT>
-__device__ __forceinline__ void store_thread(T* dst, int valid_here, bool vec, const T (&x)[VT]) {
-  if(vec) {
-    constexpr int per = 16 / sizeof(T);
-#pragma unroll
-    for(int q = 0; q < VT / per; ++q) {
-      uint4 w;
-      memcpy(&w, &x[q * per], 16);
-      reinterpret_cast<uint4*>(dst)[q] = w;
-    }
-  } else {
-#pragma unroll
-    for(int i = 0; i < VT; ++i) if(i < valid_here) dst[i] = x[i];
-  }
-}
-
 // Warp-striped vector layout of a tile: warp w owns elements
 // [w * 32 * VT, (w + 1) * 32 * VT) of the tile; in row r of that range lane l
 // holds the PER = 16 / sizeof(T) consecutive elements starting at
@@ -355,7 +320,7 @@ struct striped_t {
 // the warp-striped layout and each warp scans its range in registers; warp 0
 // scans the warp totals, publishes the tile aggregate and looks back; the
 // carry-in is added and the tile stored with the same striped layout.
-template<typename T, typename op_t, int NT, int VT, bool exclusive, int LBK = 1, int MINB = 1>
+template<typename T, typename op_t, int NT, int VT, bool exclusive, int MINB = 1>
 __global__ void __launch_bounds__(NT, MINB)
 scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T> st,
   uint32_t* tile_counter, T* reduction, int* error, int vec_ok) {
@@ -399,50 +364,25 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   }
   if(lane == 0) warp_tot[warp] = acc;
   __syncthreads();
-  T carry;
-  if constexpr(LBK == 0) {
-    // Every thread derives the tile aggregate and its warp's offset.
-    __shared__ T s_val[NW];
-    __shared__ int s_info[NW];
-    T wexc = op_t::identity(), tile_agg = op_t::identity();
-#pragma unroll
-    for(int w = 0; w < NW; ++w) {
-      const T t = warp_tot[w];
-      if(w < warp) wexc = op(wexc, t);
-      tile_agg = op(tile_agg, t);
-    }
+  if(warp == 0) {
+    T t = lane < NW ? warp_tot[lane] : op_t::identity();
+    T tinc = warp_inclusive_scan(t, op);
+    const T tile_agg = __shfl_sync(0xffffffffu, tinc, NW - 1);
     T prefix;
     if(tile == 0) {
       prefix = init;
-      if(tid == 0) st.publish(0, status_inclusive, op(init, tile_agg));
+      if(lane == 0) st.publish(0, status_inclusive, op(init, tile_agg));
     } else {
-      if(tid == 0) st.publish(tile, status_aggregate, tile_agg);
-      prefix = lookback_cta<NW, T>(st, tile, op, error, s_val, s_info);
-      if(tid == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
+      if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
+      prefix = lookback_warp<1, T>(st, tile, op, error);
+      if(lane == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
     }
-    if(tid == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
-    carry = op(prefix, wexc);
-  } else {
-    if(warp == 0) {
-      T t = lane < NW ? warp_tot[lane] : op_t::identity();
-      T tinc = warp_inclusive_scan(t, op);
-      const T tile_agg = __shfl_sync(0xffffffffu, tinc, NW - 1);
-      T prefix;
-      if(tile == 0) {
-        prefix = init;
-        if(lane == 0) st.publish(0, status_inclusive, op(init, tile_agg));
-      } else {
-        if(lane == 0) st.publish(tile, status_aggregate, tile_agg);
-        prefix = lookback_warp<LBK, T>(st, tile, op, error);
-        if(lane == 0) st.publish(tile, status_inclusive, op(prefix, tile_agg));
-      }
-      T texc = __shfl_up_sync(0xffffffffu, tinc, 1);
-      if(lane < NW) warp_tot[lane] = lane ? op(prefix, texc) : prefix;
-      if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
-    }
-    __syncthreads();
-    carry = warp_tot[warp];
+    T texc = __shfl_up_sync(0xffffffffu, tinc, 1);
+    if(lane < NW) warp_tot[lane] = lane ? op(prefix, texc) : prefix;
+    if(lane == 0 && reduction && base + TILE >= count) *reduction = op(prefix, tile_agg);
   }
+  __syncthreads();
+  const T carry = warp_tot[warp];
 #pragma unroll
   for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
   S::store(out + base, valid, vec, warp, lane, x);

@@ -25,18 +25,18 @@ template<typename T> using minimum_t = device::min_t<T>;
 // looping over tiles with a deferred look-back, scan_defer_kernel; 0: one
 // tile per CTA, scan_kernel), CTAs per SM asked of the compiler.
 template<int bytes> struct scan_tuning;
-template<> struct scan_tuning<4> { enum { nt = 256, vt = 32, stages = 1, minb = 4 }; };
-template<> struct scan_tuning<8> { enum { nt = 512, vt = 16, stages = 1, minb = 2 }; };
+template<> struct scan_tuning<4> { enum { nt = 256, vt = 32, persistent = 1, minb = 4 }; };
+template<> struct scan_tuning<8> { enum { nt = 512, vt = 16, persistent = 1, minb = 2 }; };
 
 template<scan_type_t scan_type = scan_type_exc,
-  int nt = 0, int vt = 0, int stages = -1, int lbk = 0, int minb = -1, typename T,
+  int nt = 0, int vt = 0, int persistent = -1, int minb = -1, typename T,
   typename op_t = plus_t<T>>
 status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
   T* out, T init = op_t::identity(), op_t op = op_t(), T* reduction = nullptr) {
   using namespace device;
   constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
   constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
-  constexpr int STAGES = stages >= 0 ? stages : (int)scan_tuning<sizeof(T)>::stages;
+  constexpr int PERSISTENT = persistent >= 0 ? persistent : (int)scan_tuning<sizeof(T)>::persistent;
   constexpr int MINB = minb >= 0 ? minb : (int)scan_tuning<sizeof(T)>::minb;
   constexpr int tile = NT * VT;
   if(count < 0) return MGPU_ERR_INVALID_ARG;
@@ -60,7 +60,7 @@ status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int
   status.bind(base + status_off, num_tiles);
   int vec = aligned16_host(in) && aligned16_host(out);
   const char* name = scan_type == scan_type_exc ? "scan_exc" : "scan_inc";
-  if constexpr(STAGES > 0) {
+  if constexpr(PERSISTENT > 0) {
     typedef scan_defer_layout<T, NT, VT> DL;
     auto k = scan_defer_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, MINB>;
     if(!ctx.allow_smem(k, DL::bytes)) return MGPU_ERR_CUDA;
@@ -74,7 +74,7 @@ status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int
     });
   } else {
     return ctx.launch(name, [&] {
-      scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, lbk, MINB>
+      scan_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, MINB>
         <<<(unsigned)num_tiles, NT, 0, ctx.stream>>>(in, out, count, init, op, status,
           (uint32_t*)base, reduction, ctx.d_error, vec);
     });
@@ -83,11 +83,11 @@ status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int
 
 // The reference's in-place form: scan(aux_data, aux_size, cmd, data, count,
 // init, op) is exclusive (vk/scan.hxx:12-13).
-template<scan_type_t scan_type = scan_type_exc, int nt = 0, int vt = 0, int stages = -1,
+template<scan_type_t scan_type = scan_type_exc, int nt = 0, int vt = 0, int persistent = -1,
   typename T, typename op_t = plus_t<T>>
 status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t count,
   T init = op_t::identity(), op_t op = op_t()) {
-  return scan<scan_type, nt, vt, stages>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
+  return scan<scan_type, nt, vt, persistent>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
 }
 
 // Memcache form.
