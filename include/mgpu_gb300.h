@@ -314,6 +314,15 @@ MGPU_API mgpu_status_t mgpu_profile_read(mgpu_context_t* ctx, char* names, size_
 /* Kernel launches issued on this context since creation. */
 MGPU_API int64_t mgpu_launch_count(mgpu_context_t* ctx);
 
+/* ---- failure-path self test (no reference counterpart) ----
+ * Enqueues one kernel that waits, with at most `limit` polls each, on an
+ * mbarrier phase and on a device flag that nothing completes -- the two kinds
+ * of bounded wait the primitives use (bulk-copy completion, look-back).  The
+ * waits give up, record MGPU_ERR_LOOKBACK_TIMEOUT in the context's error word
+ * and the kernel returns, so the next mgpu_synchronize reports that status and
+ * the context stays usable.  limit: 1 .. 2^22. */
+MGPU_API mgpu_status_t mgpu_selftest_bounded_wait(mgpu_context_t* ctx, int limit);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,9 +170,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait on an mbarrier phase.  Returns false (and raises the error)
-// if the limit was reached; the caller then must not read the staged data.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* error) {
-  for(int it = 0; it < spin_limit; ++it) {
+// if `limit` polls pass without completion; the caller then must not read
+// the staged data.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* error,
+  int limit = spin_limit) {
+  for(int it = 0; it < limit; ++it) {
     if(mbar_try_wait(bar, parity)) return true;
   }
   raise_error(error, err_lookback_timeout);

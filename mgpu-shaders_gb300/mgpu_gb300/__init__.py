@@ -122,6 +122,11 @@ class Context:
     def launch_count(self):
         return lib().mgpu_launch_count(self._h)
 
+    def selftest_bounded_wait(self, limit=4096):
+        """Enqueues the bounded-wait self test; the next synchronize() raises
+        MgpuError with status 3 (a bounded wait gave up)."""
+        self._check(lib().mgpu_selftest_bounded_wait(self._h, limit))
+
     # --- launch-shape tuning ---
     def tuning_variants(self, primitive, key_dtype):
         buf = ctypes.create_string_buffer(512)

@@ -77,6 +77,7 @@ _SIGS = {
     "mgpu_profile_enable": ([_VP, _I32], _I32),
     "mgpu_profile_read": ([_VP, _VP, ctypes.c_size_t, _VP, _VP, _I32, _VP], _I32),
     "mgpu_launch_count": ([_VP], _I64),
+    "mgpu_selftest_bounded_wait": ([_VP, _I32], _I32),
 }
 
 
