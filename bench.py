@@ -118,6 +118,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(ms, pg, device="cuda"):
+    """The slowest rank's time: replicas sort independently (no exchange), so
+    the job takes as long as its slowest rank."""
+    if pg is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -844,11 +855,7 @@ def main():
     clk = clocks.stop()
     ctx.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = sum(step_ms) / steps
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(step_ms) / steps, pg)
 
     # Correctness of the last timed output (cheap properties).
     gk = copies[(steps - 1) % 2][0].numpy()

@@ -1,0 +1,62 @@
+"""Multi-GPU runs are independent replicas (no data-path collective): the
+bench takes the slowest rank's time and rank 0 alone reports.  Checked here
+with two gloo ranks on the CPU."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+_WORKER = r"""
+import os, sys, json
+sys.path.insert(0, sys.argv[1])
+import torch.distributed as dist
+import bench
+dist.init_process_group("gloo")
+rank = dist.get_rank()
+ms = bench.max_over_ranks(10.0 + 5.0 * rank, dist, device="cpu")
+print(json.dumps({"rank": rank, "ms": ms, "info": bench.dist_info()}))
+dist.barrier()
+dist.destroy_process_group()
+"""
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_max_over_ranks_with_two_gloo_ranks(tmp_path):
+    pytest.importorskip("torch.distributed")
+    worker = tmp_path / "worker.py"
+    worker.write_text(_WORKER)
+    port = _free_port()
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
+                   RANK=str(rank), WORLD_SIZE="2", LOCAL_RANK=str(rank))
+        procs.append(subprocess.Popen([sys.executable, str(worker), REPO], env=env,
+                                      stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                                      text=True))
+    outs = []
+    for p in procs:
+        out, err = p.communicate(timeout=120)
+        assert p.returncode == 0, err
+        outs.append(out.strip().splitlines()[-1])
+    import json
+    res = sorted((json.loads(o) for o in outs), key=lambda r: r["rank"])
+    assert [r["ms"] for r in res] == [15.0, 15.0]
+    assert [r["info"] for r in res] == [[0, 2, 0], [1, 2, 1]]
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    p = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True,
+                       text=True, timeout=120)
+    assert p.returncode == 0
+    assert p.stdout.strip() == ""
