@@ -391,7 +391,9 @@ seg_onesweep_pass(onesweep_args<K, V> a, const int64_t* offsets, seg_state_t s, 
 // head, since nothing before it reaches this tile.
 
 // First segment whose begin offset is >= each tile's first element.
-__global__ inline void seg_tile_first(const int64_t* offsets, int64_t num_segments, int64_t tile,
+// (A template, so that every translation unit may include it.)
+template<int NT = 256>
+__global__ void seg_tile_first(const int64_t* offsets, int64_t num_segments, int64_t tile,
   int64_t num_tiles, int* first) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if(t >= num_tiles) return;

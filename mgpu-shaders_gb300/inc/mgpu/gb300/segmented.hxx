@@ -156,7 +156,7 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   if(ctx.check(cudaMemsetAsync(base, 0, head_bytes, ctx.stream))) return MGPU_ERR_CUDA;
   int* first = (int*)(base + first_off);
   st = ctx.launch("seg_tile_first", [&] {
-    seg_tile_first<<<(unsigned)div_up(num_tiles, 256), 256, 0, ctx.stream>>>(offsets,
+    seg_tile_first<256><<<(unsigned)div_up(num_tiles, 256), 256, 0, ctx.stream>>>(offsets,
       num_segments, TILE, num_tiles, first);
   });
   if(st) return st;
