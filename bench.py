@@ -785,7 +785,7 @@ def main():
                     help="key entropy of the headline radix workload")
     ap.add_argument("--workload", default="radix", choices=["radix"] + sorted(WORKLOADS))
     ap.add_argument("--serve-pool", type=int, default=24)
-    ap.add_argument("--serve-reps", type=int, default=3)
+    ap.add_argument("--serve-reps", type=int, default=60)
     ap.add_argument("--serve-max-log2", type=int, default=26)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-budget-gb", type=int, default=64)

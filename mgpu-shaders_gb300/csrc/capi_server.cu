@@ -51,6 +51,7 @@ struct mgpu_server {
   int num_slots = 0;
   std::vector<mgpu_context*> slots;
   std::vector<char> slot_busy;
+  int* h_err = nullptr;          // pinned: each slot's device error word after a request
   mgpu_context* sizing = nullptr;
   cudaMemPool_t pool = nullptr;
 
@@ -171,6 +172,12 @@ struct mgpu_server {
         return MGPU_ERR_INVALID_ARG;
     }
     release(rec);
+    // The slot's device error word travels back (and is cleared) in stream
+    // order, so the completion needs no host synchronisation.
+    if(cudaMemcpyAsync(h_err + rec->slot, c->ctx.d_error, sizeof(int), cudaMemcpyDeviceToHost,
+         s) != cudaSuccess ||
+       cudaMemsetAsync(c->ctx.d_error, 0, sizeof(int), s) != cudaSuccess)
+      return MGPU_ERR_CUDA;
     callback_arg* arg = new(std::nothrow) callback_arg { this, rec->id };
     if(!arg) return MGPU_ERR_OOM;
     if(cudaLaunchHostFunc(s, on_complete, arg) != cudaSuccess) { delete arg; return MGPU_ERR_CUDA; }
@@ -212,11 +219,9 @@ struct mgpu_server {
         uint64_t id = completions.front();
         completions.pop_front();
         request_record* rec = records[id];
-        int slot = rec->slot;
-        lk.unlock();
-        mgpu_status_t st = mgpu_synchronize(slots[slot]);   // stream idle: reads the error word
-        lk.lock();
-        finish_locked(rec, st);
+        // The callback ran after the slot's error word reached h_err.
+        const int e = h_err[rec->slot];
+        finish_locked(rec, e ? (mgpu_status_t)e : MGPU_OK);
       }
       if(stop && queue.empty() && in_flight == 0) break;
       bool progressed = false;
@@ -297,6 +302,14 @@ mgpu_status_t mgpu_server_create(int device, size_t budget_bytes, int num_slots,
     delete s;
     return st;
   }
+  if(cudaMallocHost(&s->h_err, sizeof(int) * num_slots) != cudaSuccess) {
+    for(auto* c : s->slots) mgpu_context_destroy(c);
+    mgpu_context_destroy(s->sizing);
+    cudaMemPoolDestroy(s->pool);
+    delete s;
+    return MGPU_ERR_OOM;
+  }
+  for(int i = 0; i < num_slots; ++i) s->h_err[i] = 0;
   s->slot_busy.assign(num_slots, 0);
   s->scheduler = std::thread([s] { s->run(); });
   *out = s;
@@ -415,6 +428,7 @@ mgpu_status_t mgpu_server_destroy(mgpu_server_t* s) {
   for(auto* c : s->slots) mgpu_context_destroy(c);
   if(s->sizing) mgpu_context_destroy(s->sizing);
   if(s->pool) cudaMemPoolDestroy(s->pool);
+  if(s->h_err) cudaFreeHost(s->h_err);
   delete s;
   return MGPU_OK;
 }
