@@ -9,7 +9,7 @@ One step = one in-place radix sort of 2^28 key/value pairs through the C ABI
 flush is needed.  `value` is device throughput (Mkeys/s from the mean of the
 per-step event times); `e2e` is the same metric through the C ABI with the
 keys/values starting and ending in pinned host memory (uploads, sorts and
-downloads on three streams over two buffer sets, so neighbouring steps'
+downloads on three streams over three buffer sets, so neighbouring steps'
 copies overlap each sort).
 `roofline` covers the dominant kernel (onesweep_pass): 16 algorithmic bytes
 per key per launch, divided by its mean event-timed duration.
@@ -887,13 +887,15 @@ def main():
     # End to end through the C ABI: every step copies its keys and values from
     # pinned host memory, sorts them and copies the result back, as a caller
     # streaming sorts would pipeline them: uploads, sorts and downloads run on
-    # three streams (one context each) over two device buffer sets, so step
+    # three streams (one context each) over three device buffer sets, so step
     # i + 1's upload and step i - 1's download overlap step i's sort.
     e2e_steps = max(4, min(steps, 6))
     hk = torch.from_numpy(keys_h).pin_memory()
     hv = torch.from_numpy(vals_h).pin_memory()
+    nbuf = 3
+    bufs = copies + [(mg.DeviceArray(n, np.uint32), mg.DeviceArray(n, np.uint32))]
     outs = [(torch.empty_like(hk).pin_memory(), torch.empty_like(hv).pin_memory())
-            for _ in range(2)]
+            for _ in range(nbuf)]
     lib = mg.lib()
     nbytes = 4 * n
     streams = [torch.cuda.Stream() for _ in range(3)]          # upload, sort, download
@@ -905,10 +907,10 @@ def main():
         e0.record(stream)
         for st_ in streams:
             st_.wait_event(e0)
-        freed = [None, None]     # download of the buffer set's previous step done
+        freed = [None] * nbuf    # download of the buffer set's previous step done
         for i in range(num_steps):
-            b = i % 2
-            dk, dv = copies[b]
+            b = i % nbuf
+            dk, dv = bufs[b]
             if freed[b] is not None:
                 streams[0].wait_event(freed[b])
             up._check(lib.mgpu_memcpy(up.handle, dk.ptr, hk.data_ptr(), nbytes))
