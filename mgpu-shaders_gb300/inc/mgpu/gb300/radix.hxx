@@ -133,26 +133,28 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
   return MGPU_OK;
 }
 
-// Keys-only form (the reference's signature, vk/radix.hxx:197-198).
-template<
-  int nt = radix_tuning<sizeof(uint32_t)>::nt,
-  int vt = radix_tuning<sizeof(uint32_t)>::vt,
-  int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
-  typename K>
+// Keys-only form with the reference's signature (vk/radix.hxx:195-198):
+// radix_sort<nt, vt, num_bits>(aux_data, aux_size, ctx, keys, count).  In the
+// reference nt, vt and num_bits (4 or 8) only choose the launch shape and the
+// digit width -- the resulting permutation is the same for all of them -- so
+// they are accepted for source compatibility and the shape tuned for the key
+// width runs (8-bit digits).
+template<int nt = 0, int vt = 0, int num_bits = 8, typename K>
 status_t radix_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* keys, int64_t count) {
-  return radix_sort_kv<nt, vt, min_blocks>(aux_data, &aux_size, ctx, keys,
-    (device::no_values*)nullptr, count);
+  static_assert(num_bits >= 1 && num_bits <= 8, "digit width of the reference's template");
+  constexpr int b = sizeof(K);
+  return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
+    aux_data, &aux_size, ctx, keys, (device::no_values*)nullptr, count);
 }
 
-// Key-value form.
-template<
-  int nt = radix_tuning<sizeof(uint32_t)>::nt,
-  int vt = radix_tuning<sizeof(uint32_t)>::vt,
-  int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
-  typename K, typename V>
+// Key-value form (an addition: the reference sorts keys only).
+template<int nt = 0, int vt = 0, int num_bits = 8, typename K, typename V>
 status_t radix_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* keys, V* vals,
   int64_t count) {
-  return radix_sort_kv<nt, vt, min_blocks>(aux_data, &aux_size, ctx, keys, vals, count);
+  static_assert(num_bits >= 1 && num_bits <= 8, "digit width of the reference's template");
+  constexpr int b = sizeof(K);
+  return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
+    aux_data, &aux_size, ctx, keys, vals, count);
 }
 
 // Memcache forms: aux comes from the context's grow-only cache.
