@@ -90,6 +90,17 @@ status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t
   return scan<scan_type, nt, vt, persistent>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
 }
 
+// The reference's exact template shape, scan<nt, vt>(aux_data, aux_size,
+// cmd, data, count, init, op) (vk/scan.hxx:10-13): there nt and vt only choose
+// the launch shape, so the in-place exclusive scan runs with the shape tuned
+// for the element width.  (nt and vt have no defaults here, so a call without
+// template arguments selects the form above.)
+template<int nt, int vt, typename T, typename op_t = plus_t<T>>
+status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t count,
+  T init = op_t::identity(), op_t op = op_t()) {
+  return scan<scan_type_exc>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
+}
+
 // Memcache form.
 template<scan_type_t scan_type = scan_type_exc, typename T, typename op_t = plus_t<T>>
 status_t scan(context_t& ctx, const T* in, int64_t count, T* out, T init = op_t::identity(),

@@ -55,7 +55,8 @@ int main() {
     CHECK(ok, "launch_transform");
   }
 
-  // mergesort_keys with a user comparator (stable).
+  // mergesort_keys with a user comparator (stable), in the reference's
+  // default launch shape <128, 7> (vk/mergesort.hxx).
   {
     const int count = 10000;
     std::vector<float> h(count);
@@ -65,9 +66,9 @@ int main() {
     context.memcpy(gpu, h.data(), sizeof(float) * count);
     void* aux_data = nullptr;
     size_t aux_size = 0;
-    mergesort_keys(aux_data, aux_size, cmd_buffer, gpu, count, abs_greater_t());
+    mergesort_keys<128, 7>(aux_data, aux_size, cmd_buffer, gpu, count, abs_greater_t());
     aux_data = context.alloc_gpu(aux_size);
-    mergesort_keys(aux_data, aux_size, cmd_buffer, gpu, count, abs_greater_t());
+    mergesort_keys<128, 7>(aux_data, aux_size, cmd_buffer, gpu, count, abs_greater_t());
     std::vector<float> got(count);
     context.memcpy(got.data(), gpu, sizeof(float) * count);
     if(context.synchronize()) return 2;
@@ -90,9 +91,9 @@ int main() {
     context.memcpy(b, bh.data(), sizeof(float) * b_count);
     void* aux_data = nullptr;
     size_t aux_size = 0;
-    merge(aux_data, aux_size, cmd_buffer, a, a_count, b, b_count, c, less_t<float>());
+    merge<128, 7>(aux_data, aux_size, cmd_buffer, a, a_count, b, b_count, c, less_t<float>());
     aux_data = context.alloc_gpu(aux_size);
-    merge(aux_data, aux_size, cmd_buffer, a, a_count, b, b_count, c, less_t<float>());
+    merge<128, 7>(aux_data, aux_size, cmd_buffer, a, a_count, b, b_count, c, less_t<float>());
     std::vector<float> got(count), ref(count);
     context.memcpy(got.data(), c, sizeof(float) * count);
     if(context.synchronize()) return 2;
@@ -117,6 +118,15 @@ int main() {
     bool ok = true;
     for(int i = 0; i < count; ++i) ok &= h[i] == (int)((int64_t)i * (i - 1) / 2);
     CHECK(ok, "scan_exclusive_in_place");
+    // The same call with the reference's explicit launch knobs and operator.
+    for(int i = 0; i < count; ++i) h[i] = i;
+    context.memcpy(gpu, h.data(), sizeof(int) * count);
+    scan<128, 7>(aux_data, aux_size, context, gpu, count, 0, plus_t<int>());
+    context.memcpy(h.data(), gpu, sizeof(int) * count);
+    if(context.synchronize()) return 2;
+    ok = true;
+    for(int i = 0; i < count; ++i) ok &= h[i] == (int)((int64_t)i * (i - 1) / 2);
+    CHECK(ok, "scan_reference_template_shape");
   }
 
   // Keys-only radix sort, sorted six times (examples/vk_radix2/vk_radix2.cxx).
