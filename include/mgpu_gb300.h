@@ -12,6 +12,8 @@
  *
  * as in vk/merge.hxx:30-34, vk/mergesort.hxx:35-41, vk/scan.hxx:19-22,54-59
  * and vk/radix.hxx:288-302 (where `aux_data == nullptr` only grows aux_size).
+ * aux must start on a 16-byte boundary (device allocations do); a misaligned
+ * aux or one smaller than the sizing pass asked for is MGPU_ERR_INVALID_ARG.
  * With aux_size == NULL the context's grow-only device cache supplies the
  * memory (the reference's memcache_t, vk/context.hxx:110-134).
  *

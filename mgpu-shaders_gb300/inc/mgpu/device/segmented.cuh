@@ -388,23 +388,23 @@ seg_onesweep_pass(onesweep_args<K, V> a, const int64_t* offsets, seg_state_t s, 
 // with the operator (fa, a) . (fb, b) = (fa | fb, fb ? b : a op b), which is
 // associative, so one chained scan restarts at every segment head.  A tile's
 // look-back also stops early at any predecessor whose aggregate contains a
-// head, since nothing before it reaches this tile.
+// head, since nothing before it reaches this tile.  As for the plain scan,
+// `op` must be associative and commutative (plus, min, max): a tile's
+// aggregate folds its elements in thread order, not element order.
 
-// First segment whose begin offset is >= each tile's first element.
-// (A template, so that every translation unit may include it.)
+// Head bitmap of a segmented scan: bit e of words[e / 32] is set when a
+// non-empty segment begins at element e (element 0 always begins one).  One
+// thread per segment; `words` is zeroed before the launch.  (A template, so
+// that every translation unit may include it.)
 template<int NT = 256>
-__global__ void seg_tile_first(const int64_t* offsets, int64_t num_segments, int64_t tile,
-  int64_t num_tiles, int* first) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if(t >= num_tiles) return;
-  int64_t pos = t * tile;
-  int64_t lo = 0, hi = num_segments;   // lower_bound over offsets[0, num_segments)
-  while(lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if(offsets[mid] < pos) lo = mid + 1;
-    else hi = mid;
-  }
-  first[t] = (int)lo;
+__global__ void seg_mark_heads(const int64_t* offsets, int64_t num_segments, int64_t count,
+  uint32_t* words) {
+  const int64_t sg = (int64_t)blockIdx.x * NT + threadIdx.x;
+  if(sg == 0) atomicOr(&words[0], 1u);
+  if(sg >= num_segments) return;
+  const int64_t o = offsets[sg];
+  if(o > 0 && o < count && offsets[sg + 1] > o)
+    atomicOr(&words[o >> 5], 1u << (o & 31));
 }
 
 template<typename T>
@@ -509,23 +509,26 @@ __device__ seg_pair_t<T> seg_lookback_cta(const seg_status_t<T>& st, int64_t til
 }
 
 // Segmented scan with the deferred look-back of scan_defer_kernel: resident
-// CTAs loop over tiles; in one iteration a tile's values arrive by bulk copy,
-// its segment heads are marked and its (head, value) aggregate published; in
-// the next the CTA looks back, publishes the tile's inclusive pair, re-reads
-// the values from L2 and writes the scanned tile.  Elements are held in the
-// warp-striped layout of striped_t.
+// CTAs loop over tiles; in one iteration a tile's values and its words of the
+// head bitmap arrive by bulk copy and its (head, value) aggregate is
+// published; in the next the CTA looks back, publishes the tile's inclusive
+// pair, re-reads the values from L2 and writes the scanned tile.  Elements
+// are held in the warp-striped layout of striped_t.  The bitmap holds one
+// word per 32 elements, padded to whole tiles.
 template<typename T, int NT, int VT>
 struct seg_scan_defer_layout {
+  static constexpr int head_words = NT * VT / 32;
   static constexpr size_t stage_bytes = sizeof(T) * NT * VT;
-  static constexpr size_t bar_off = stage_bytes;
+  static constexpr size_t heads_off = stage_bytes;
+  static constexpr size_t bar_off = heads_off + sizeof(uint32_t) * head_words;
   static constexpr size_t bytes = bar_off + 16;
+  static_assert(head_words % 4 == 0, "bulk-copy granularity");
 };
 
 template<typename T, typename op_t, int NT, int VT, bool exclusive, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
-seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets,
-  int64_t num_segments, const int* tile_first, T init, op_t op, seg_status_t<T> st,
-  uint32_t* tile_counter, int* error, int vec_ok) {
+seg_scan_defer_kernel(const T* in, T* out, int64_t count, const uint32_t* head_bits,
+  T init, op_t op, seg_status_t<T> st, uint32_t* tile_counter, int* error, int vec_ok) {
   typedef striped_t<T, VT> S;
   typedef seg_pair_t<T> P;
   typedef seg_scan_defer_layout<T, NT, VT> L;
@@ -552,8 +555,9 @@ seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets
   auto fetch = [&](int64_t id) {
     s_id = id;
     if(id < bulk_tiles) {
-      mbar_arrive_expect_tx(bar, (uint32_t)L::stage_bytes);
+      mbar_arrive_expect_tx(bar, (uint32_t)(L::stage_bytes + sizeof(uint32_t) * HW));
       bulk_load(smem, in + id * TILE, (uint32_t)L::stage_bytes, bar);
+      bulk_load(smem + L::heads_off, head_bits + id * HW, (uint32_t)(sizeof(uint32_t) * HW), bar);
     }
   };
   // Head bits of this thread's PER elements of row r.
@@ -579,24 +583,10 @@ seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets
     const bool have_cur = cur < num_tiles;
 
     if(have_cur) {
-      // Mark the heads of the non-empty segments that start in `cur`.
       const int64_t base = cur * TILE;
       const int valid = (int)min((int64_t)TILE, count - base);
-      uint32_t* h = heads[hb];
-      for(int i = tid; i < HW; i += NT) h[i] = 0;
-      __syncthreads();
-      for(int64_t sg = tile_first[cur] + tid; sg < num_segments; sg += NT) {
-        const int64_t o = offsets[sg];
-        if(o >= base + valid) break;
-        if(offsets[sg + 1] > o && o >= base) {
-          const int r = (int)(o - base);
-          atomicOr(&h[r >> 5], 1u << (r & 31));
-        }
-      }
-      if(cur == 0 && tid == 0) atomicOr(&h[0], 1u);
-      __syncthreads();
-      // Ordered fold of the tile's pairs.
       T x[VT];
+      const uint32_t* hs = head_bits + cur * HW;
       if(cur < bulk_tiles) {
         mbar_wait_bounded(bar, parity, error);   // a timeout raised the error
         parity ^= 1;
@@ -606,25 +596,27 @@ seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets
           uint4 w = *reinterpret_cast<const uint4*>(sx + S::offset(warp, lane, r));
           memcpy(&x[r * PER], &w, 16);
         }
+        hs = (const uint32_t*)(smem + L::heads_off);
       } else {
         S::load(in + base, valid, false, warp, lane, x, op_t::identity());
       }
-      P acc { op_t::identity(), 0u };
+      // Keep the tile's head words for its scan in the next iteration.
+      for(int i = tid; i < HW; i += NT) heads[hb][i] = hs[i];
+      // The warp's (head, value) pair: a head if its range holds one, and the
+      // fold of its elements from its last head (or its first element) on.
+      // The warp's range is words [warp * VT, warp * VT + VT) of the tile.
+      const uint32_t hw = lane < VT ? hs[warp * VT + lane] : 0u;
+      const int last = __reduce_max_sync(0xffffffffu, hw ? lane * 32 + 31 - __clz(hw) : -1);
+      T a = op_t::identity();
 #pragma unroll
       for(int r = 0; r < ROWS; ++r) {
-        const uint32_t hr = row_heads(h, r);
-        P l { op_t::identity(), 0u };
+        const int e = S::offset(warp, lane, r) - warp * 32 * VT;
 #pragma unroll
-        for(int j = 0; j < PER; ++j) l = seg_combine<T>(l, P { x[r * PER + j], (hr >> j) & 1u }, op);
-#pragma unroll
-        for(int off = 1; off < 32; off <<= 1) {
-          P y { __shfl_down_sync(0xffffffffu, l.v, off), __shfl_down_sync(0xffffffffu, l.f, off) };
-          if(lane + off < 32) l = seg_combine<T>(l, y, op);
-        }
-        acc = seg_combine<T>(acc, P { __shfl_sync(0xffffffffu, l.v, 0),
-          __shfl_sync(0xffffffffu, l.f, 0) }, op);
+        for(int j = 0; j < PER; ++j)
+          if(e + j >= last) a = op(a, x[r * PER + j]);
       }
-      if(lane == 0) { wv[warp] = acc.v; wf[warp] = acc.f; }
+      a = warp_reduce(a, op);
+      if(lane == 0) { wv[warp] = a; wf[warp] = last >= 0; }
     }
     __syncthreads();                           // stage consumed; warp totals visible
     if(tid == copy_tid) fetch(next_id);
@@ -652,25 +644,31 @@ seg_scan_defer_kernel(const T* in, T* out, int64_t count, const int64_t* offsets
       }
       // Per row: the pair before this lane's first element, counted from the
       // start of the warp's range.
+      // Each row is scanned with value-only shuffles: the lanes' head bits
+      // (one ballot) give every lane the first lane of its segment in the
+      // row, and a lane combines only partial results from that lane on.
       P before[ROWS];
       P acc { op_t::identity(), 0u };
+      const uint32_t lt = lanemask_lt();
 #pragma unroll
       for(int r = 0; r < ROWS; ++r) {
         const uint32_t hr = row_heads(h, r);
-        P l { op_t::identity(), 0u };
+        T inc = op_t::identity();              // this lane's elements after its last head
 #pragma unroll
-        for(int j = 0; j < PER; ++j) l = seg_combine<T>(l, P { x[r * PER + j], (hr >> j) & 1u }, op);
-        P inc = l;
+        for(int j = 0; j < PER; ++j)
+          inc = ((hr >> j) & 1u) ? x[r * PER + j] : op(inc, x[r * PER + j]);
+        const uint32_t mask = __ballot_sync(0xffffffffu, hr != 0);
+        const uint32_t upto = mask & (lt | (1u << lane));
+        const int start = upto ? 31 - __clz(upto) : -1;   // segment's first lane in the row
 #pragma unroll
         for(int off = 1; off < 32; off <<= 1) {
-          P y { __shfl_up_sync(0xffffffffu, inc.v, off), __shfl_up_sync(0xffffffffu, inc.f, off) };
-          if(lane >= off) inc = seg_combine<T>(y, inc, op);
+          const T y = __shfl_up_sync(0xffffffffu, inc, off);
+          if(lane - off >= max(start, 0)) inc = op(y, inc);
         }
-        P ex { __shfl_up_sync(0xffffffffu, inc.v, 1), __shfl_up_sync(0xffffffffu, inc.f, 1) };
-        if(lane == 0) ex = P { op_t::identity(), 0u };
-        before[r] = seg_combine<T>(acc, ex, op);
-        acc = seg_combine<T>(acc, P { __shfl_sync(0xffffffffu, inc.v, 31),
-          __shfl_sync(0xffffffffu, inc.f, 31) }, op);
+        T exv = __shfl_up_sync(0xffffffffu, inc, 1);
+        if(lane == 0) exv = op_t::identity();
+        before[r] = seg_combine<T>(acc, P { exv, (mask & lt) ? 1u : 0u }, op);
+        acc = seg_combine<T>(acc, P { __shfl_sync(0xffffffffu, inc, 31), mask ? 1u : 0u }, op);
       }
       if(lane == 0) { wv[warp] = acc.v; wf[warp] = acc.f; }
       __syncthreads();

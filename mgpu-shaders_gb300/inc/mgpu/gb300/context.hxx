@@ -260,7 +260,11 @@ inline bool resolve_aux(context_t& ctx, void* aux_data, size_t* aux_size, size_t
     return false;
   }
   if(!aux_data) { *aux_size += needed; return true; }
-  if(*aux_size < needed) { status = MGPU_ERR_INVALID_ARG; return true; }
+  // The kernels bulk-copy from aux and update 8-byte words in it.
+  if(*aux_size < needed || ((uintptr_t)aux_data & 15)) {
+    status = MGPU_ERR_INVALID_ARG;
+    return true;
+  }
   base = (char*)aux_data;
   return false;
 }

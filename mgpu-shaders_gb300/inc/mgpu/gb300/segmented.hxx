@@ -7,8 +7,8 @@
 //   sort: memset, classify, persistent small-segment sort, then for the
 //         segments larger than one tile a histogram launch and one onesweep
 //         pass per 8-bit digit over all of their tiles together;
-//   scan: memset, per-tile segment lookup, one persistent look-back scan
-//         (seg_scan_defer_kernel).
+//   scan: memset, head bitmap (one thread per segment), one persistent
+//         look-back scan (seg_scan_defer_kernel).
 // No host synchronisation; graph-capturable.
 #pragma once
 
@@ -136,7 +136,7 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   using namespace device;
   constexpr int NT = 256;
   constexpr int VT = sizeof(T) == 4 ? 32 : 16;
-  constexpr int MINB = 3;
+  constexpr int MINB = sizeof(T) == 4 ? 3 : 2;   // 8-byte values spill at 3
   constexpr int TILE = NT * VT;
   if(count < 0 || num_segments < 0 || num_segments > INT32_MAX) return MGPU_ERR_INVALID_ARG;
   const int64_t num_tiles = div_up(count, TILE);
@@ -144,9 +144,9 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   aux_layout_t lay;
   size_t cnt_off = lay.add(16);
   size_t flags_off = lay.add(sizeof(uint32_t) * num_tiles);
+  size_t bits_off = lay.add(sizeof(uint32_t) * (TILE / 32) * num_tiles);
   size_t head_bytes = lay.total;
   size_t vals_off = lay.add(2 * sizeof(uint64_t) * num_tiles);
-  size_t first_off = lay.add(sizeof(int) * num_tiles);
   char* base = nullptr;
   status_t st;
   if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
@@ -154,10 +154,10 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   if(!in || !out || !offsets || num_segments == 0) return MGPU_ERR_INVALID_ARG;
   (void)cnt_off;
   if(ctx.check(cudaMemsetAsync(base, 0, head_bytes, ctx.stream))) return MGPU_ERR_CUDA;
-  int* first = (int*)(base + first_off);
-  st = ctx.launch("seg_tile_first", [&] {
-    seg_tile_first<256><<<(unsigned)div_up(num_tiles, 256), 256, 0, ctx.stream>>>(offsets,
-      num_segments, TILE, num_tiles, first);
+  uint32_t* bits = (uint32_t*)(base + bits_off);
+  st = ctx.launch("seg_mark_heads", [&] {
+    seg_mark_heads<256><<<(unsigned)div_up(num_segments, 256), 256, 0, ctx.stream>>>(offsets,
+      num_segments, count, bits);
   });
   if(st) return st;
   seg_status_t<T> status { (uint32_t*)(base + flags_off), (uint64_t*)(base + vals_off),
@@ -170,8 +170,8 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   const int64_t grid = std::min<int64_t>((int64_t)per_sm * ctx.sm_count, num_tiles);
   const int vec = aligned16_host(in) && aligned16_host(out);
   return ctx.launch("seg_scan", [&] {
-    k<<<(unsigned)grid, NT, SL::bytes, ctx.stream>>>(in, out, count, offsets, num_segments,
-      first, init, op, status, (uint32_t*)base, ctx.d_error, vec);
+    k<<<(unsigned)grid, NT, SL::bytes, ctx.stream>>>(in, out, count, bits, init, op, status,
+      (uint32_t*)base, ctx.d_error, vec);
   });
 }
 

@@ -94,6 +94,15 @@ def test_radix_two_phase_aux(mgpu, ctx, oracle, rng):
     assert np.array_equal(dk.numpy(), ok) and np.array_equal(dv.numpy(), ov)
     with pytest.raises(mgpu.MgpuError):
         ctx.radix_sort(dk, dv, aux=(aux.data_ptr(), size - 1))
+    # aux that does not start on 16 bytes is rejected before any launch.
+    aux2 = torch.empty(size + 16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(mgpu.MgpuError):
+        ctx.radix_sort(dk, dv, aux=(aux2.data_ptr() + 4, size))
+    dsrc = mgpu.DeviceArray.from_numpy(np.arange(1000, dtype=np.int32))
+    seg = mgpu.DeviceArray.from_numpy(np.array([0, 400, 1000], dtype=np.int64))
+    with pytest.raises(mgpu.MgpuError):
+        ctx.segmented_scan(dsrc, dsrc, seg, aux=(aux2.data_ptr() + 8, size))
+    ctx.synchronize()
 
 
 def test_radix_unaligned_pointers(mgpu, ctx, oracle, rng):
