@@ -418,28 +418,48 @@ __device__ __forceinline__ seg_pair_t<T> seg_combine(seg_pair_t<T> a, seg_pair_t
   return { b.f ? b.v : op(a.v, b.v), a.f | b.f };
 }
 
-// Status of a tile: flag word (status | head << 2) and one value word per
+// Status of a tile.  4-byte values: one 64-bit word per tile, (status |
+// head << 2) over the value bits, so one load returns a consistent pair.
+// 8-byte values: a flag word (status | head << 2) and one value word per
 // status ([2][tiles]: aggregate slot, inclusive slot), so a reader always
-// loads the value that belongs to the flag it observed.
+// loads the value that belongs to the flag it observed.  `flags` holds
+// 8 bytes per tile (zeroed before the scan) in both cases.
 template<typename T>
 struct seg_status_t {
   uint32_t* flags;
   uint64_t* values;
   int64_t tiles;
+  static constexpr bool packed = sizeof(T) <= 4;
   __device__ __forceinline__ void publish(int64_t tile, uint32_t status, seg_pair_t<T> p) const {
-    uint64_t b = 0;
-    memcpy(&b, &p.v, sizeof(T));
-    st_relaxed(values + (status == status_inclusive ? tiles : 0) + tile, b);
-    st_release(flags + tile, status | (p.f << 2));
+    if constexpr(packed) {
+      uint32_t b = 0;
+      memcpy(&b, &p.v, sizeof(T));
+      st_relaxed((uint64_t*)flags + tile, ((uint64_t)(status | (p.f << 2)) << 32) | b);
+    } else {
+      uint64_t b = 0;
+      memcpy(&b, &p.v, sizeof(T));
+      st_relaxed(values + (status == status_inclusive ? tiles : 0) + tile, b);
+      st_release(flags + tile, status | (p.f << 2));
+    }
   }
   __device__ __forceinline__ uint32_t read(int64_t tile, seg_pair_t<T>& p) const {
-    uint32_t w = ld_acquire(flags + tile);
-    if(w & 3) {
-      uint64_t b = ld_relaxed(values + ((w & 3) == status_inclusive ? tiles : 0) + tile);
-      memcpy(&p.v, &b, sizeof(T));
-      p.f = (w >> 2) & 1;
+    if constexpr(packed) {
+      const uint64_t w = ld_relaxed((const uint64_t*)flags + tile);
+      const uint32_t f = (uint32_t)(w >> 32), b = (uint32_t)w;
+      if(f & 3) {
+        memcpy(&p.v, &b, sizeof(T));
+        p.f = (f >> 2) & 1;
+      }
+      return f & 3;
+    } else {
+      uint32_t w = ld_acquire(flags + tile);
+      if(w & 3) {
+        uint64_t b = ld_relaxed(values + ((w & 3) == status_inclusive ? tiles : 0) + tile);
+        memcpy(&p.v, &b, sizeof(T));
+        p.f = (w >> 2) & 1;
+      }
+      return w & 3;
     }
-    return w & 3;
   }
 };
 

@@ -134,19 +134,22 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   int64_t count, T* out, const int64_t* offsets, int64_t num_segments,
   T init = op_t::identity(), op_t op = op_t()) {
   using namespace device;
+  // 8192-element tiles at 3 CTAs/SM for 4-byte values (measured against 4
+  // CTAs/SM and 4096-element tiles); 8-byte values spill above 2 CTAs/SM.
   constexpr int NT = 256;
   constexpr int VT = sizeof(T) == 4 ? 32 : 16;
-  constexpr int MINB = sizeof(T) == 4 ? 3 : 2;   // 8-byte values spill at 3
+  constexpr int MINB = sizeof(T) == 4 ? 3 : 2;
   constexpr int TILE = NT * VT;
+  constexpr bool packed = seg_status_t<T>::packed;
   if(count < 0 || num_segments < 0 || num_segments > INT32_MAX) return MGPU_ERR_INVALID_ARG;
   const int64_t num_tiles = div_up(count, TILE);
   if(num_tiles > 0x7fffffffll) return MGPU_ERR_INVALID_ARG;
   aux_layout_t lay;
   size_t cnt_off = lay.add(16);
-  size_t flags_off = lay.add(sizeof(uint32_t) * num_tiles);
+  size_t flags_off = lay.add(sizeof(uint64_t) * num_tiles);
   size_t bits_off = lay.add(sizeof(uint32_t) * (TILE / 32) * num_tiles);
   size_t head_bytes = lay.total;
-  size_t vals_off = lay.add(2 * sizeof(uint64_t) * num_tiles);
+  size_t vals_off = packed ? 0 : lay.add(2 * sizeof(uint64_t) * num_tiles);
   char* base = nullptr;
   status_t st;
   if(resolve_aux(ctx, aux_data, aux_size, lay.total, base, st)) return st;
@@ -160,8 +163,8 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
       num_segments, count, bits);
   });
   if(st) return st;
-  seg_status_t<T> status { (uint32_t*)(base + flags_off), (uint64_t*)(base + vals_off),
-    num_tiles };
+  seg_status_t<T> status { (uint32_t*)(base + flags_off),
+    packed ? nullptr : (uint64_t*)(base + vals_off), num_tiles };
   typedef seg_scan_defer_layout<T, NT, VT> SL;
   auto k = seg_scan_defer_kernel<T, op_t, NT, VT, scan_type == scan_type_exc, MINB>;
   if(!ctx.allow_smem(k, SL::bytes)) return MGPU_ERR_CUDA;
