@@ -189,6 +189,20 @@ __device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, 
     :: "r"(smem_addr(smem_dst)), "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
+// Asynchronous copy of one naturally aligned 4-, 8- or 16-byte element
+// global -> shared (cp.async); cp_async_wait_all() waits for this thread's
+// copies.
+template<typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gmem_src) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "cp.async element size");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;"
+    :: "r"(smem_addr(smem_dst)), "l"(gmem_src), "n"((int)sizeof(T)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 __device__ __forceinline__ bool aligned16(const void* p) {
   return 0 == ((uintptr_t)p & 15);
 }

@@ -102,6 +102,11 @@ __device__ __forceinline__ void warp_rank_sort(K* keys, V* vals, int n) {
 // Stable LSD radix sort (8-bit digits) of n <= 32 * W * ITEMS keys held in a
 // shared-memory slice, by a group of W warps.  gtid is the thread's index in
 // the group; hist has W * 256 words; tmp has W words.  Keys are radix bits.
+// The ceil(n / 32) rows of 32 keys are spread evenly over the warps (warp w
+// ranks rows [w * rpw, (w + 1) * rpw), so a short segment does not wait on
+// one warp's long chain); rows past n are skipped (the last partial row pads
+// with all-ones keys, which rank after every real key and land past n).
+// Peers come from one ballot per digit bit.
 template<int W, int ITEMS, typename U, typename V>
 __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* hist,
   uint32_t* tmp, int passes, int gtid) {
@@ -110,34 +115,40 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
   constexpr int DPT = G >= radix_bins ? 1 : radix_bins / G;   // digits per thread
   static_assert(G >= radix_bins ? G % radix_bins == 0 : radix_bins % G == 0, "group size");
   const int lane = gtid & 31, gw = gtid >> 5;
-  const int warp_base = gw * 32 * ITEMS;
+  const int rpw = min(ITEMS, (((n + 31) >> 5) + W - 1) / W);         // rows per warp
+  const int warp_base = gw * 32 * rpw;
   const int rem = n - warp_base - lane;
+  const int rows = min(rpw, max(0, (n - warp_base + 31) >> 5));      // warp-uniform
   const uint32_t lt_mask = lanemask_lt();
   auto gsync = [] { if(W == 1) __syncwarp(); else __syncthreads(); };
   for(int pass = 0; pass < passes; ++pass) {
     const int shift = 8 * pass;
     for(int i = gtid; i < W * radix_bins; i += G) hist[i] = 0;
     U k[ITEMS];
-    V v[ITEMS];
 #pragma unroll
-    for(int i = 0; i < ITEMS; ++i) {
-      bool in = 32 * i < rem;
-      k[i] = in ? ks[warp_base + 32 * i + lane] : ~(U)0;
-      if constexpr(HAS_V) v[i] = in ? vs[warp_base + 32 * i + lane] : V();
-    }
+    for(int i = 0; i < ITEMS; ++i)
+      if(i < rows) k[i] = 32 * i < rem ? ks[warp_base + 32 * i + lane] : ~(U)0;
     gsync();
     uint32_t r[ITEMS];
     uint32_t* wh = hist + gw * radix_bins;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
-      uint32_t d = extract_digit(k[i], shift, 8);
-      uint32_t peers = __match_any_sync(0xffffffffu, d);
-      uint32_t below = peers & lt_mask;
-      uint32_t cnt = wh[d];
-      __syncwarp();
-      if(!below) wh[d] = cnt + __popc(peers);
-      __syncwarp();
-      r[i] = cnt + __popc(below);
+      if(i < rows) {
+        const uint32_t d = extract_digit(k[i], shift, 8);
+        uint32_t peers = 0xffffffffu;
+#pragma unroll
+        for(int b = 0; b < 8; ++b) {
+          const bool bit = (d >> b) & 1u;
+          const uint32_t m = __ballot_sync(0xffffffffu, bit);
+          peers &= bit ? m : ~m;
+        }
+        const uint32_t below = peers & lt_mask;
+        const uint32_t cnt = wh[d];
+        __syncwarp();
+        if(!below) wh[d] = cnt + __popc(peers);
+        __syncwarp();
+        r[i] = cnt + __popc(below);
+      }
     }
     gsync();
     uint32_t tot[DPT];
@@ -177,12 +188,24 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
       excl += tot[j];
     }
     gsync();
+    // Keys first; values are read from their old places only after that
+    // (fewer live registers), then scattered after a barrier.
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
-      uint32_t d = extract_digit(k[i], shift, 8);
-      uint32_t pos = r[i] + wh[d];
-      ks[pos] = k[i];
-      if constexpr(HAS_V) vs[pos] = v[i];
+      if(i < rows) {
+        r[i] += wh[extract_digit(k[i], shift, 8)];
+        ks[r[i]] = k[i];
+      }
+    }
+    if constexpr(HAS_V) {
+      V v[ITEMS];
+#pragma unroll
+      for(int i = 0; i < ITEMS; ++i)
+        if(i < rows) v[i] = 32 * i < rem ? vs[warp_base + 32 * i + lane] : V();
+      gsync();
+#pragma unroll
+      for(int i = 0; i < ITEMS; ++i)
+        if(i < rows) vs[r[i]] = v[i];
     }
     gsync();
   }
@@ -230,10 +253,36 @@ radix_sort_cta(K* keys, V* vals, int n) {
   }
 }
 
+// Copies the n keys (as radix bits) and values of one segment into shared
+// memory, STRIDE threads, t = this thread's index.  Asynchronous element
+// copies (cp.async) put every load of the segment in flight at once, so the
+// segment costs one memory latency rather than one per row, and hold no
+// registers.  Each thread waits for its own copies and converts its own
+// keys; the caller's barrier publishes the result.
+template<int STRIDE, typename K, typename V, typename U>
+__device__ __forceinline__ void seg_stage_in(const K* keys, const V* vals, int n, U* ks, V* vs,
+  int t) {
+  constexpr bool HAS_V = !std::is_same<V, no_values>::value;
+  constexpr bool async_v = HAS_V && (sizeof(V) == 4 || sizeof(V) == 8 || sizeof(V) == 16);
+  for(int i = t; i < n; i += STRIDE) {
+    cp_async_elem(ks + i, (const U*)keys + i);
+    if constexpr(async_v) cp_async_elem(vs + i, vals + i);
+    else if constexpr(HAS_V) vs[i] = vals[i];
+  }
+  cp_async_wait_all();
+  if constexpr(!(std::is_integral<K>::value && std::is_unsigned<K>::value)) {
+    for(int i = t; i < n; i += STRIDE) {
+      K key;
+      memcpy(&key, &ks[i], sizeof(K));
+      ks[i] = radix_key<K>::to_bits(key);
+    }
+  }
+}
+
 // Persistent sort of every segment up to one tile: CTA-class segments first
 // (whole CTA), then slice-class and warp-class segments (one warp each).
-template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES>
-__global__ void __launch_bounds__(NT)
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB)
 seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
   typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
   typedef typename L::U U;
@@ -257,10 +306,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int seg = s.cta_list[item];
     const int64_t b = offsets[seg];
     const int n = (int)(offsets[seg + 1] - b);
-    for(int i = tid; i < n; i += NT) {
-      ks[i] = radix_key<K>::to_bits(keys[b + i]);
-      if constexpr(HAS_V) vs[i] = vals[b + i];
-    }
+    seg_stage_in<NT>(keys + b, HAS_V ? vals + b : vals, n, ks, vs, tid);
     __syncthreads();
     group_radix_sort<NT / 32, ITEMS>(ks, vs, n, hist, tmp, PASSES, tid);
     for(int i = tid; i < n; i += NT) {
@@ -283,10 +329,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int seg = s.slice_list[item];
     const int64_t b = offsets[seg];
     const int n = (int)(offsets[seg + 1] - b);
-    for(int i = lane; i < n; i += 32) {
-      wks[i] = radix_key<K>::to_bits(keys[b + i]);
-      if constexpr(HAS_V) wvs[i] = vals[b + i];
-    }
+    seg_stage_in<32>(keys + b, HAS_V ? vals + b : vals, n, wks, wvs, lane);
     __syncwarp();
     group_radix_sort<1, SLICE_ITEMS>(wks, wvs, n, wh, nullptr, PASSES, lane);
     for(int i = lane; i < n; i += 32) {

@@ -29,6 +29,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   constexpr int NT = T::nt, ITEMS = T::vt, MINB = T::min_blocks;
   constexpr int TILE = NT * ITEMS;
   constexpr int SLICE_ITEMS = ITEMS;
+  constexpr int SMALL_MINB = 1;
   constexpr int SLICE = 32 * SLICE_ITEMS;
   constexpr int PASSES = sizeof(K);
   constexpr bool has_values = !std::is_same<V, no_values>::value;
@@ -76,9 +77,11 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   });
   if(st) return st;
 
-  auto small = seg_small_sort<K, V, NT, ITEMS, SLICE_ITEMS, PASSES>;
+  auto small = seg_small_sort<K, V, NT, ITEMS, SLICE_ITEMS, PASSES, SMALL_MINB>;
   if(!ctx.allow_smem(small, SL::bytes)) return MGPU_ERR_CUDA;
-  int sgrid = ctx.sm_count * 4;
+  const int per_sm = ctx.resident_ctas(small, NT, SL::bytes);
+  if(per_sm < 1) return MGPU_ERR_CUDA;
+  const int sgrid = ctx.sm_count * per_sm;
   st = ctx.launch("seg_small_sort", [&] {
     small<<<sgrid, NT, SL::bytes, ctx.stream>>>(keys, vals, offsets, s);
   });
