@@ -65,9 +65,11 @@ struct onesweep_layout {
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
   static constexpr int tile = NT * ITEMS;
   static constexpr int num_warps = NT / 32;
+  // The key and value buffers carry 16 spare bytes: a tile that does not
+  // start on 16 bytes is bulk-copied as the aligned window around it.
   static constexpr size_t keys_off = 0;
-  static constexpr size_t vals_off = keys_off + sizeof(U) * tile;
-  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
+  static constexpr size_t vals_off = keys_off + sizeof(U) * tile + 16;
+  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile + 16 : 0);
   static constexpr size_t gbase_off = hist_off + sizeof(uint32_t) * num_warps * radix_bins;
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
@@ -76,6 +78,10 @@ struct onesweep_layout {
   // Each warp's slice of the key buffer (32 * ITEMS keys) doubles as its two
   // banks of 256 match masks while it ranks, when it is large enough.
   static constexpr bool match_in_slice = sizeof(U) * 32 * ITEMS >= 2 * 256 * sizeof(uint32_t);
+  // A window copy shifts the staged keys by up to 16 bytes, and the ranking
+  // words by as much; they must still end before the next warp's keys.
+  static constexpr bool window_ok =
+    !match_in_slice || sizeof(U) * 32 * ITEMS >= 2 * 256 * sizeof(uint32_t) + 16;
   static_assert(NT >= radix_bins && NT % 32 == 0, "one thread per digit");
   static_assert((sizeof(U) * tile) % 16 == 0, "bulk-copy granularity");
 };
@@ -280,18 +286,26 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const int64_t base = t.base;
   const int valid = t.valid;
   const int tile = t.local;
-  // a.tma: both arrays start on 16 bytes; a tile qualifies when it is full
-  // and starts on a whole vector of keys and of values.
-  constexpr int64_t vec_mask = (16 / sizeof(U) > (HAS_V ? 16 / sizeof(V) : 1) ?
-    16 / sizeof(U) : (HAS_V ? 16 / sizeof(V) : 1)) - 1;
-  const bool bulk = a.tma && valid == TILE && 0 == (base & vec_mask);
+  // a.tma: both arrays start on 16 bytes.  A full tile is bulk-copied as
+  // the 16-byte-aligned window [kstart, kend) around it (the tile starts
+  // koff elements in); values likewise.  The window must lie inside the
+  // arrays (count elements), else the tile takes plain loads.
+  constexpr int64_t KV = 16 / sizeof(U);
+  constexpr int64_t VV = HAS_V ? 16 / sizeof(V) : 1;
+  const int64_t kstart = base & ~(KV - 1), vstart = base & ~(VV - 1);
+  const int64_t kend = (base + TILE + KV - 1) & ~(KV - 1);
+  const int64_t vend = (base + TILE + VV - 1) & ~(VV - 1);
+  const bool bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count) &&
+    (L::window_ok || (kstart == base && vstart == base));
+  const int koff = bulk ? (int)(base - kstart) : 0;
+  const int voff = bulk ? (int)(base - vstart) : 0;
 
   if(bulk && tid == 0) {
-    constexpr uint32_t kbytes = sizeof(U) * TILE;
-    constexpr uint32_t vbytes = HAS_V ? sizeof(V) * TILE : 0;
+    const uint32_t kbytes = (uint32_t)(sizeof(U) * (kend - kstart));
+    const uint32_t vbytes = HAS_V ? (uint32_t)(sizeof(V) * (vend - vstart)) : 0u;
     mbar_arrive_expect_tx(bar, kbytes + vbytes);
-    bulk_load(ks, a.keys_in + base, kbytes, bar);
-    if(HAS_V) bulk_load(vs, a.vals_in + base, vbytes, bar);
+    bulk_load(ks, a.keys_in + kstart, kbytes, bar);
+    if(HAS_V) bulk_load(vs, a.vals_in + vstart, vbytes, bar);
   }
 
   // Concentration of this pass's digits: when some digit holds more than
@@ -324,7 +338,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       return;
     }
 #pragma unroll
-    for(int i = 0; i < ITEMS; ++i) k[i] = ks[warp_base + 32 * i + lane];
+    for(int i = 0; i < ITEMS; ++i) k[i] = ks[koff + warp_base + 32 * i + lane];
   } else {
     __syncthreads();
     const U* src = a.keys_in + base + warp_base + lane;
@@ -355,10 +369,14 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   uint32_t r[ITEMS];
   uint32_t* wh = whist + warp * radix_bins;
   const uint32_t lt_mask = lanemask_lt();
+  // Each warp's ranking words start `moff` elements into its slice: at or
+  // after the end of the previous warp's staged keys (which that warp may
+  // still be reading) and on 16 bytes (they are cleared with 16-byte stores).
+  const int moff = (int)((koff + KV - 1) & ~(KV - 1));
   // Where warp w's count of digit d sits after ranking.
   auto warp_count = [&](int w, int d) -> uint32_t {
     if constexpr(L::match_in_slice)
-      return ((const uint32_t*)(ks + w * 32 * ITEMS))[2 * d + 1 - ((d >> 4) & 1)];
+      return ((const uint32_t*)(ks + moff + w * 32 * ITEMS))[2 * d + 1 - ((d >> 4) & 1)];
     else return whist[w * radix_bins + d];
   };
   if constexpr(L::match_in_slice) {
@@ -369,7 +387,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     // back the advanced count with a clear mask.  Three shared-memory
     // operations per key.  Digits with bit 4 set keep their mask in the upper
     // half, so the masks of any 32 digits spread over all 32 banks.
-    uint32_t* mw = (uint32_t*)(ks + warp_base);
+    uint32_t* mw = (uint32_t*)(ks + moff + warp_base);
     __syncwarp();
     for(int j = lane; j < 2 * radix_bins / 4; j += 32)
       reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
@@ -463,7 +481,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     V v[ITEMS];
     if(bulk) {
 #pragma unroll
-      for(int i = 0; i < ITEMS; ++i) v[i] = vs[warp_base + 32 * i + lane];
+      for(int i = 0; i < ITEMS; ++i) v[i] = vs[voff + warp_base + 32 * i + lane];
     } else {
       const V* src = a.vals_in + base + warp_base + lane;
 #pragma unroll
