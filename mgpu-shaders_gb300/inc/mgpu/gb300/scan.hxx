@@ -7,6 +7,10 @@
 // common/cta_scan.hxx:63-66), an out-of-place overload, an optional device
 // reduction output, and reduce().  `init` enters once, as the left-most
 // operand: exclusive out[0] = init; inclusive out[i] = init (+) in[0..i].
+// `op` must be associative and commutative with an identity() (plus_t,
+// maximum_t, minimum_t): a tile's aggregate folds each thread's elements
+// before the warps' partials, not in element order.  Float sums therefore
+// round differently from a sequential sum (within the usual bound).
 #pragma once
 
 #include "context.hxx"

@@ -132,6 +132,8 @@ status_t segmented_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* key
   return segmented_sort_kv(aux_data, &aux_size, ctx, keys, vals, count, offsets, num_segments);
 }
 
+// Scan of each segment independently (exclusive: a segment's first output
+// is init).  `op` as for scan(): associative and commutative.
 template<scan_type_t scan_type = scan_type_inc, typename T, typename op_t = plus_t<T>>
 status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in,
   int64_t count, T* out, const int64_t* offsets, int64_t num_segments,
