@@ -111,6 +111,17 @@ MGPU_API mgpu_status_t mgpu_memset(mgpu_context_t* ctx, void* dest, int value, s
 MGPU_API mgpu_status_t mgpu_radix_sort(mgpu_context_t* ctx, mgpu_dtype_t key_type, void* keys,
   int val_bytes, void* vals, int64_t count, void* aux_data, size_t* aux_size);
 
+/* The same sort with the number of keys read on the device from *d_count
+ * (clamped to [0, max_count]) when the kernels run, so one captured graph
+ * (mgpu_graph_begin/end) replays for any size up to max_count without
+ * re-capture; keys, vals and aux are sized for max_count, and elements past
+ * *d_count are left as they are.  The reference's GL mergesort keeps its
+ * pass state in device memory for the same reason (gl/mergesort.hxx:23-27,
+ * 48-54).  d_count == NULL is MGPU_ERR_INVALID_ARG. */
+MGPU_API mgpu_status_t mgpu_radix_sort_count_on_device(mgpu_context_t* ctx,
+  mgpu_dtype_t key_type, void* keys, int val_bytes, void* vals, int64_t max_count,
+  const int64_t* d_count, void* aux_data, size_t* aux_size);
+
 /* ---- merge (vk::merge key-value and keys-only, vk/merge.hxx:12-59) ----
  * Stable merge of sorted A and B into C (ties take A first, bounds_lower,
  * common/cta_merge.hxx:23-25).  vals may be NULL with val_bytes 0. */

@@ -6,14 +6,16 @@ using namespace mgpu::gb300;
 using mgpu::device::no_values;
 
 mgpu_status_t radix_sort_w64(mgpu_context* c, mgpu_dtype_t key_type, void* keys, int val_bytes,
-  void* vals, int64_t count, int variant, void* aux, size_t* aux_size) {
+  void* vals, int64_t count, int variant, void* aux, size_t* aux_size, const int64_t* d_count) {
   auto go_key = [&](auto* kp) -> mgpu_status_t {
     typedef std::remove_pointer_t<decltype(kp)> K;
     auto go = [&](auto* vp) -> mgpu_status_t {
       typedef std::remove_pointer_t<decltype(vp)> V;
       switch(variant) {
-        case 1: return radix_sort_kv<256, 8, 4>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
-        default: return radix_sort_kv<256, 12, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
+        case 1: return radix_sort_kv<256, 8, 4>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+          d_count);
+        default: return radix_sort_kv<256, 12, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+          d_count);
       }
     };
     if(val_bytes == 0) return go((no_values*)nullptr);

@@ -57,6 +57,9 @@ struct onesweep_args {
   int first;                 // convert K -> bits on load
   int last;                  // convert bits -> K on store
   int tma;                   // pointers allow 16-byte bulk copies
+  // If set, the number of keys is read here at kernel start (clamped to
+  // [0, count]); `count` is then the capacity the launch was sized for.
+  const int64_t* count_ptr = nullptr;
 };
 
 template<typename K, typename V, int NT, int ITEMS>
@@ -114,8 +117,10 @@ __device__ __forceinline__ void scan_256_pair(uint32_t& x, uint32_t& y, uint32_t
 // per bin and CTA.  Dynamic shared memory: PASSES * 256 * LANES counters.
 template<typename K, int NT, int PASSES, int LANES>
 __global__ void __launch_bounds__(NT)
-radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised) {
+radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised,
+  const int64_t* count_ptr) {
   typedef typename radix_key<K>::bits_t U;
+  if(count_ptr) count = max((int64_t)0, min(*count_ptr, count));
   constexpr int BINS = PASSES * radix_bins;
   extern __shared__ __align__(16) uint32_t sh[];
   const int tid = threadIdx.x;
@@ -545,7 +550,12 @@ __global__ void __launch_bounds__(NT, MIN_BLOCKS)
 onesweep_pass(onesweep_args<K, V> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int TILE = NT * ITEMS;
+  // A count read from device memory: the grid covers the capacity, and CTAs
+  // that claim a tile id past the last tile leave (ids are claimed in order,
+  // so no tile waits on them).
+  if(a.count_ptr) a.count = max((int64_t)0, min(*a.count_ptr, a.count));
   const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
+  if((int64_t)tile * TILE >= a.count) return;
   onesweep_tile_t t;
   t.base = (int64_t)tile * TILE;
   t.valid = (int)min((int64_t)TILE, a.count - t.base);

@@ -36,7 +36,7 @@ template<
   int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
   typename K, typename V>
 status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys, V* vals,
-  int64_t count) {
+  int64_t count, const int64_t* d_count = nullptr) {
   using namespace device;
   typedef typename radix_key<K>::bits_t U;
   constexpr bool has_values = !std::is_same<V, no_values>::value;
@@ -46,8 +46,11 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
 
   if(count < 0 || count > radix_max_count) return MGPU_ERR_INVALID_ARG;
 
+  // With d_count the number of keys is read on the device (at most `count`,
+  // the capacity everything is sized for), so one captured graph serves any
+  // size up to it.
   int64_t num_tiles = div_up(count, tile);
-  if(num_tiles <= 1) {
+  if(num_tiles <= 1 && !d_count) {
     // One tile: the whole sort runs in shared memory in one CTA; no aux.
     char* unused = nullptr;
     status_t s0;
@@ -95,7 +98,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     int grid = (int)std::min<int64_t>(std::max<int64_t>(want, 1), (int64_t)ctx.sm_count);
     int vec = aligned16_host(keys);
     st = ctx.launch("radix_histogram", [&] {
-      hk<<<grid, hnt, hsmem, ctx.stream>>>(keys, count, hist, vec);
+      hk<<<grid, hnt, hsmem, ctx.stream>>>(keys, count, hist, vec, d_count);
     });
     if(st) return st;
   }
@@ -120,6 +123,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     a.first = p == 0;
     a.last = p == passes - 1;
     a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));
+    a.count_ptr = d_count;
     // Clear this pass's look-back words right before it runs, so they are
     // still in L2 when tiles poll them.
     if(ctx.check(cudaMemsetAsync(a.lookback, 0, sizeof(uint32_t) * num_tiles * radix_bins,

@@ -198,13 +198,20 @@ class Context:
                                           None, count, None, ctypes.byref(size)))
         return size.value
 
-    def radix_sort(self, keys, vals=None, aux=None):
-        """In-place stable radix sort of DeviceArray keys (and vals)."""
+    def radix_sort(self, keys, vals=None, aux=None, device_count=None):
+        """In-place stable radix sort of DeviceArray keys (and vals).  With
+        `device_count` (a device pointer to one int64) the number of keys is
+        read on the device when the kernels run; keys.count is the capacity."""
         a, s = self._aux_args(aux)
-        self._check(lib().mgpu_radix_sort(
-            self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr),
-            0 if vals is None else vals.dtype.itemsize,
-            None if vals is None else ctypes.c_void_p(vals.ptr), keys.count, a, s))
+        vb = 0 if vals is None else vals.dtype.itemsize
+        vp = None if vals is None else ctypes.c_void_p(vals.ptr)
+        if device_count is None:
+            self._check(lib().mgpu_radix_sort(
+                self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr), vb, vp, keys.count, a, s))
+        else:
+            self._check(lib().mgpu_radix_sort_count_on_device(
+                self._h, DTYPES[keys.dtype], ctypes.c_void_p(keys.ptr), vb, vp, keys.count,
+                ctypes.c_void_p(device_count), a, s))
 
     def merge(self, a_keys, a_vals, b_keys, b_vals, c_keys, c_vals, comp="less", aux=None):
         a, s = self._aux_args(aux)

@@ -43,6 +43,7 @@ _SIGS = {
     "mgpu_memcpy": ([_VP, _VP, _VP, ctypes.c_size_t], _I32),
     "mgpu_memset": ([_VP, _VP, _I32, ctypes.c_size_t], _I32),
     "mgpu_radix_sort": ([_VP, _I32, _VP, _I32, _VP, _I64, _VP, _SZ], _I32),
+    "mgpu_radix_sort_count_on_device": ([_VP, _I32, _VP, _I32, _VP, _I64, _VP, _VP, _SZ], _I32),
     "mgpu_merge": ([_VP, _I32, _VP, _VP, _I64, _VP, _VP, _I64, _VP, _VP, _I32, _I32, _VP, _SZ],
                    _I32),
     "mgpu_mergesort": ([_VP, _I32, _VP, _I32, _VP, _I64, _I32, _VP, _SZ], _I32),

@@ -41,6 +41,46 @@ def test_radix_sort_graph_replay(mgpu, gctx, oracle, rng):
     g.close()
 
 
+def test_radix_sort_graph_count_on_device(mgpu, gctx, oracle, rng):
+    """One graph captured at a capacity replays for any count written to
+    device memory between replays; elements past the count stay as they
+    are."""
+    ctx = gctx
+    import torch
+    cap = 400_000
+    dk = mgpu.DeviceArray(cap, np.uint32)
+    dv = mgpu.DeviceArray(cap, np.uint32)
+    dcount = torch.zeros(1, dtype=torch.int64, device="cuda")
+    size = ctx.radix_sort_aux_size(np.uint32, np.uint32, cap)
+    aux = torch.empty(size, dtype=torch.uint8, device="cuda")
+    ctx.synchronize()
+    ctx.graph_begin()
+    ctx.radix_sort(dk, dv, aux=(aux.data_ptr(), size), device_count=dcount.data_ptr())
+    g = ctx.graph_end()
+    for count in (cap, 1, 0, 5120, 5121, 77_777, cap - 3):
+        k = rng.integers(0, 2 ** 32, cap, dtype=np.uint64).astype(np.uint32)
+        v = np.arange(cap, dtype=np.uint32)
+        dk.copy_from(mgpu.DeviceArray.from_numpy(k))
+        dv.copy_from(mgpu.DeviceArray.from_numpy(v))
+        dcount.fill_(count)
+        torch.cuda.synchronize()
+        g.launch()
+        ctx.synchronize()
+        ok, ov = oracle.radix_sort(k[:count], v[:count])
+        gk, gv = dk.numpy(), dv.numpy()
+        assert np.array_equal(gk[:count], ok) and np.array_equal(gv[:count], ov), count
+        assert np.array_equal(gk[count:], k[count:]) and np.array_equal(gv[count:], v[count:])
+    # A count above the capacity is clamped to it.
+    k = rng.integers(0, 2 ** 32, cap, dtype=np.uint64).astype(np.uint32)
+    dk.copy_from(mgpu.DeviceArray.from_numpy(k))
+    dcount.fill_(cap + 12345)
+    torch.cuda.synchronize()
+    g.launch()
+    ctx.synchronize()
+    assert np.array_equal(dk.numpy(), np.sort(k))
+    g.close()
+
+
 def test_mergesort_graph_with_reserved_cache(mgpu, gctx, oracle, rng):
     ctx = gctx
     import torch
