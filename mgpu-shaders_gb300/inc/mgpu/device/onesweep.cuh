@@ -545,17 +545,19 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
 }
 
-template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int WINDOW = 4>
+template<typename K, typename V, int NT, int ITEMS, int MIN_BLOCKS, int WINDOW = 4,
+  bool DEV_COUNT = false>
 __global__ void __launch_bounds__(NT, MIN_BLOCKS)
 onesweep_pass(onesweep_args<K, V> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int TILE = NT * ITEMS;
-  // A count read from device memory: the grid covers the capacity, and CTAs
-  // that claim a tile id past the last tile leave (ids are claimed in order,
-  // so no tile waits on them).
-  if(a.count_ptr) a.count = max((int64_t)0, min(*a.count_ptr, a.count));
+  // DEV_COUNT: the count is read from device memory; the grid covers the
+  // capacity, and CTAs that claim a tile id past the last tile leave (ids
+  // are claimed in order, so no tile waits on them).
+  if constexpr(DEV_COUNT) a.count = max((int64_t)0, min(*a.count_ptr, a.count));
   const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
-  if((int64_t)tile * TILE >= a.count) return;
+  if constexpr(DEV_COUNT)
+    if((int64_t)tile * TILE >= a.count) return;
   onesweep_tile_t t;
   t.base = (int64_t)tile * TILE;
   t.valid = (int)min((int64_t)TILE, a.count - t.base);

@@ -34,6 +34,7 @@ template<
   int nt = radix_tuning<sizeof(uint32_t)>::nt,
   int vt = radix_tuning<sizeof(uint32_t)>::vt,
   int min_blocks = radix_tuning<sizeof(uint32_t)>::min_blocks,
+  bool dev_count = false,
   typename K, typename V>
 status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys, V* vals,
   int64_t count, const int64_t* d_count = nullptr) {
@@ -46,9 +47,10 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
 
   if(count < 0 || count > radix_max_count) return MGPU_ERR_INVALID_ARG;
 
-  // With d_count the number of keys is read on the device (at most `count`,
-  // the capacity everything is sized for), so one captured graph serves any
-  // size up to it.
+  // dev_count: the number of keys is read on the device from d_count (at
+  // most `count`, the capacity everything is sized for), so one captured
+  // graph serves any size up to it.
+  if(dev_count != (d_count != nullptr)) return MGPU_ERR_INVALID_ARG;
   int64_t num_tiles = div_up(count, tile);
   if(num_tiles <= 1 && !d_count) {
     // One tile: the whole sort runs in shared memory in one CTA; no aux.
@@ -103,7 +105,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     if(st) return st;
   }
 
-  auto kernel = onesweep_pass<K, V, nt, vt, min_blocks>;
+  auto kernel = onesweep_pass<K, V, nt, vt, min_blocks, 4, dev_count>;
   if(!ctx.allow_smem(kernel, L::bytes)) return MGPU_ERR_CUDA;
 
   U* k_io[2] = { (U*)keys, alt_keys };
