@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -77,11 +78,14 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        # The raw samples go to MGPU_CLOCKS_CSV when set (to keep them),
+        # else to a temporary file.
+        self.path = os.environ.get("MGPU_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), "mgpu_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
