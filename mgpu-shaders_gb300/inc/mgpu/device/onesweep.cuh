@@ -271,7 +271,9 @@ struct lookback_window_t {
   }
 };
 
-template<typename K, typename V, int NT, int ITEMS, int WINDOW = 4>
+// UNALIGNED: tiles may start anywhere (the segmented sort's large segments);
+// a plain sort's tiles start on whole tiles, so it skips the window logic.
+template<typename K, typename V, int NT, int ITEMS, int WINDOW = 4, bool UNALIGNED = false>
 __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const onesweep_tile_t& t, unsigned char* smem) {
   typedef onesweep_layout<K, V, NT, ITEMS> L;
@@ -294,16 +296,24 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   // a.tma: both arrays start on 16 bytes.  A full tile is bulk-copied as
   // the 16-byte-aligned window [kstart, kend) around it (the tile starts
   // koff elements in); values likewise.  The window must lie inside the
-  // arrays (count elements), else the tile takes plain loads.
+  // arrays (count elements), else the tile takes plain loads.  Without
+  // UNALIGNED the tile itself must start on 16 bytes (koff = voff = 0).
   constexpr int64_t KV = 16 / sizeof(U);
   constexpr int64_t VV = HAS_V ? 16 / sizeof(V) : 1;
-  const int64_t kstart = base & ~(KV - 1), vstart = base & ~(VV - 1);
-  const int64_t kend = (base + TILE + KV - 1) & ~(KV - 1);
-  const int64_t vend = (base + TILE + VV - 1) & ~(VV - 1);
-  const bool bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count) &&
-    (L::window_ok || (kstart == base && vstart == base));
-  const int koff = bulk ? (int)(base - kstart) : 0;
-  const int voff = bulk ? (int)(base - vstart) : 0;
+  int64_t kstart = base, vstart = base, kend = base + TILE, vend = base + TILE;
+  bool bulk;
+  if constexpr(UNALIGNED) {
+    kstart = base & ~(KV - 1);
+    vstart = base & ~(VV - 1);
+    kend = (base + TILE + KV - 1) & ~(KV - 1);
+    vend = (base + TILE + VV - 1) & ~(VV - 1);
+    bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count) &&
+      (L::window_ok || (kstart == base && vstart == base));
+  } else {
+    bulk = a.tma && valid == TILE && 0 == (base & (KV - 1)) && 0 == (base & (VV - 1));
+  }
+  const int koff = UNALIGNED && bulk ? (int)(base - kstart) : 0;
+  const int voff = UNALIGNED && bulk ? (int)(base - vstart) : 0;
 
   if(bulk && tid == 0) {
     const uint32_t kbytes = (uint32_t)(sizeof(U) * (kend - kstart));

@@ -423,7 +423,7 @@ seg_onesweep_pass(onesweep_args<K, V> a, const int64_t* offsets, seg_state_t s, 
   t.lb_row = s.lookback + ((int64_t)pass * s.max_tiles + tile) * radix_bins;
   t.hist = s.seg_hist + ((int64_t)l * PASSES + pass) * radix_bins;
   t.out_base = sb;
-  onesweep_tile<K, V, NT, ITEMS>(a, t, smem);
+  onesweep_tile<K, V, NT, ITEMS, 4, true>(a, t, smem);
 }
 
 ////////////////////////////////////////////////////////////////////////////////
