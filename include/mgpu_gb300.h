@@ -2,7 +2,7 @@
  * mgpu_gb300.h - C ABI of the GB300 (sm_103a) data-parallel primitives.
  *
  * These entry points replace the host calls of seanbaxter/mgpu-shaders'
- * Vulkan API (inc/mgpu/vk/*.hxx).  Every primitive keeps the reference's
+ * Vulkan API (the inc/mgpu/vk headers).  Every primitive keeps the reference's
  * two-phase auxiliary-memory protocol:
  *
  *   size_t aux_size = 0;
