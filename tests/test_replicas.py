@@ -60,3 +60,19 @@ def test_reference_arm_other_ranks_exit_quietly():
                        text=True, timeout=120)
     assert p.returncode == 0
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_rank0_line(oracle):
+    """Rank 0 of the reference arm times the host sort and prints one JSON
+    line with the contract's keys (no GPU involved)."""
+    import json
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    p = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["metric"] and line["unit"] == "Mkeys/s"
