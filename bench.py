@@ -69,6 +69,50 @@ def make_input(n, dist="uniform", seed=SEED):
     return k, np.arange(n, dtype=np.uint32)
 
 
+def stable_sort_checks(keys, gk, gv, radix_bits=None):
+    """Properties of a key/value sort output (gk, gv) of `keys` with values =
+    original index: keys ascend (by `radix_bits` of them when given), every
+    value is a key's original index and each index appears once, and equal
+    keys keep their input order.  Together they identify the stable sort."""
+    bits = gk if radix_bits is None else radix_bits(gk)
+    n = gk.size
+    gv64 = gv.astype(np.int64)
+    in_range = bool(np.all((gv64 >= 0) & (gv64 < n)))
+    seen = np.zeros(n, dtype=bool)
+    if in_range:
+        seen[gv64] = True
+    eq = bits[1:] == bits[:-1]
+    return {
+        "keys_ascend": bool(np.all(bits[1:] >= bits[:-1])),
+        "values_are_a_permutation": in_range and bool(seen.all()),
+        "values_carry_their_keys": in_range and bool(
+            np.array_equal(keys[gv64].view(np.uint8), gk.view(np.uint8))),
+        "equal_keys_keep_input_order": bool(np.all(gv64[1:][eq] > gv64[:-1][eq])),
+    }
+
+
+def segmented_sort_checks(keys, off, gk, gv):
+    """stable_sort_checks per segment: keys ascend inside each segment, the
+    values are a permutation of the indices that keeps each index inside its
+    own segment and carries its key, and equal keys keep their input order."""
+    n = gk.size
+    seg_id = np.repeat(np.arange(len(off) - 1, dtype=np.int32), np.diff(off))
+    gv64 = gv.astype(np.int64)
+    in_range = bool(np.all((gv64 >= 0) & (gv64 < n)))
+    seen = np.zeros(n, dtype=bool)
+    if in_range:
+        seen[gv64] = True
+    same = seg_id[1:] == seg_id[:-1]
+    eq = same & (gk[1:] == gk[:-1])
+    return {
+        "keys_ascend_in_each_segment": bool(np.all(~same | (gk[1:] >= gk[:-1]))),
+        "values_are_a_permutation": in_range and bool(seen.all()),
+        "values_stay_in_their_segment": in_range and bool(np.array_equal(seg_id[gv64], seg_id)),
+        "values_carry_their_keys": in_range and bool(np.array_equal(keys[gv64], gk)),
+        "equal_keys_keep_input_order": bool(np.all(gv64[1:][eq] > gv64[:-1][eq])),
+    }
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -313,14 +357,14 @@ def wl_radix_wide(args, mg, torch, kind):
     steps, warmup = args.steps, max(3, args.warmup)
     ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
     gk, gv = work[(steps - 1) % 2][0].numpy(), work[(steps - 1) % 2][1].numpy()
-    bits = gk.view(np.uint32) if kb == 4 else gk
-    if kind != "u64":
+
+    def radix_bits(k):
+        if kind == "u64":
+            return k
         # Radix order of floats: sign-flipped bit patterns ascend.
-        b = gk.view(np.uint32)
-        bits = np.where(b >> 31 == 1, ~b, b | np.uint32(0x80000000))
-    checks = {"sorted_by_radix_bits": bool(np.all(bits[1:] >= bits[:-1])),
-              "values_permute_keys": bool(np.array_equal(keys[gv].view(np.uint8),
-                                                         gk.view(np.uint8)))}
+        b = k.view(np.uint32)
+        return np.where(b >> 31 == 1, ~b, b | np.uint32(0x80000000))
+    checks = stable_sort_checks(keys, gk, gv, radix_bits)
     passes = kb
     per_launch = {"onesweep_pass": 2 * (kb + 4) * n}
     roof, kernels = _roofline(ctx, run, restore, 3, per_launch)
@@ -483,10 +527,7 @@ def wl_segsort(args, mg, torch):
     steps, warmup = args.steps, max(3, args.warmup)
     ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
     gk, gv = wk.numpy(), wv.numpy()
-    seg_id = np.repeat(np.arange(len(off) - 1), np.diff(off))
-    order = np.lexsort((keys, seg_id))
-    checks = {"equals_per_segment_stable_sort": bool(np.array_equal(gk, keys[order]) and
-                                                     np.array_equal(gv, order.astype(np.uint32)))}
+    checks = segmented_sort_checks(keys, off, gk, gv)
     # Segments of up to one 5120-key tile sort inside seg_small_sort; larger
     # ones go through seg_onesweep_pass, one launch per digit.
     seg_lens = np.diff(off)
@@ -521,7 +562,7 @@ def wl_segsort(args, mg, torch):
     plain_loop()
     pctx.synchronize()
     loop_ms = 1e3 * (time.perf_counter() - t)
-    loop_ok = bool(np.array_equal(wk.numpy(), keys[order]))
+    loop_ok = bool(np.array_equal(wk.numpy(), gk))
     pctx.graph_begin()
     plain_loop()
     g = pctx.graph_end()
@@ -536,7 +577,7 @@ def wl_segsort(args, mg, torch):
         g.launch()
         pctx.synchronize()
         graph_ms.append(1e3 * (time.perf_counter() - t))
-    graph_ok = bool(np.array_equal(wk.numpy(), keys[order]))
+    graph_ok = bool(np.array_equal(wk.numpy(), gk))
     g.close()
     mean = sum(ms) / len(ms)
     cfg = {"workload": "segmented_sort u32 keys + u32 values, 100000 lognormal(ln 256, 2) "
@@ -768,6 +809,45 @@ WORKLOADS = {
 }
 
 
+def _summary(line):
+    """The figures of a workload line that the headline line carries."""
+    roof = line.get("roofline") or {}
+    out = {"workload": line["workload"], "value": line["value"], "unit": line["unit"],
+           "ms_per_step": line.get("ms_per_step"), "steps": line.get("steps"),
+           "step_gbs": line.get("step_gbs"), "step_frac_of_peak": line.get("step_frac_of_peak"),
+           "kernel": roof.get("kernel"), "kernel_frac_of_peak": roof.get("frac"),
+           "kernel_launch_ms": roof.get("launch_ms"),
+           "checks_pass": all(bool(v) for v in (line.get("checks") or {}).values()),
+           "clocks": line.get("clocks")}
+    if "alg_bytes_per_key" in line.get("config", {}):
+        out["alg_bytes_per_key"] = line["config"]["alg_bytes_per_key"]
+    if "inclusive" in line:
+        out["inclusive"] = line["inclusive"]
+    if "plain_calls" in line:
+        out["plain_calls"] = line["plain_calls"]
+    return out
+
+
+SECONDARY = ["radix_u64", "radix_f32", "radix_f32_normal", "mergesort", "merge", "scan_i32",
+             "scan_f32", "segsort", "segscan"]
+
+
+def run_secondary(args, mg, torch):
+    """Short timed runs (same timing rules) of every other benchmark
+    configuration, summarised for the headline line."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.n = args.secondary_steps, max(3, args.warmup), N_KEYS
+    out = {}
+    for name in SECONDARY:
+        try:
+            out[name] = _summary(WORKLOADS[name](sub, mg, torch))
+        except Exception as e:          # reported in the line, never hidden
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_workload(args):
     import torch
     import mgpu_gb300 as mg
@@ -794,6 +874,9 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the short runs of the other configurations")
+    ap.add_argument("--secondary-steps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -861,10 +944,11 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = max_over_ranks(sum(step_ms) / steps, pg)
 
-    # Correctness of the last timed output (cheap properties).
+    # Correctness of the last timed output.  With values = original index,
+    # these four properties hold for exactly one output: the stable sort.
     gk = copies[(steps - 1) % 2][0].numpy()
     gv = copies[(steps - 1) % 2][1].numpy()
-    ok_sorted = bool(np.all(gk[1:] >= gk[:-1])) and bool(np.array_equal(keys_h[gv], gk))
+    checks = stable_sort_checks(keys_h, gk, gv)
 
     # Per-kernel event timing for the roofline (same workload, fresh copies).
     prof_steps = min(steps, 4)
@@ -884,8 +968,8 @@ def main():
         peak = json.load(open(peaks_path)).get("hbm_gbs", peak)
         peak_src = "measured"
     # DRAM bytes (read + write) per key of one onesweep_pass launch, from an
-    # ncu capture of a 2^25-key launch (profiles/onesweep_pass_u32kv.md),
-    # scaled to this launch by its key count.
+    # ncu capture of a 2^25-key launch of the same kernel, scaled to this
+    # launch by its key count.
     traffic = ONESWEEP_TRAFFIC_PER_KEY * n
 
     # End to end through the C ABI: every step copies its keys and values from
@@ -969,8 +1053,15 @@ def main():
                 "steps": e2e_steps, "streams": 3, "runs_ms_per_step": e2e_runs,
                 "ms_per_step": e2e_ms},
         "clocks": clk,
-        "checks": {"timed_output_sorted_stable": ok_sorted, "e2e_output": e2e_ok},
+        "checks": dict(checks, e2e_output=e2e_ok),
     }
+    # The other benchmark configurations, each a short timed run on its own
+    # inputs (rank 0 only; the headline's buffers are released first).
+    del copies, bufs, pristine_k, pristine_v, aux_t, outs, hk, hv
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_secondary and args.n == N_KEYS:
+        line["secondary"] = run_secondary(args, mg, torch)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, reps = cpu_baseline(threads, dist=args.dist)

@@ -172,6 +172,23 @@ MGPU_API mgpu_status_t mgpu_scan_noalloc(void* stream, mgpu_dtype_t type,
   mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,
   const void* init, void* reduction);
 
+/* Device-side status of mgpu_scan_noalloc on the current device (no
+ * counterpart in the reference; it belongs to the allocation-free scan
+ * above).  mgpu_scan_noalloc has no context, so a bounded look-back wait
+ * that gave up inside it is recorded in a word of its fixed scratch array
+ * instead.  This call waits for `stream`, reads that word and clears it:
+ * MGPU_OK if no wait gave up since the last query, MGPU_ERR_LOOKBACK_TIMEOUT
+ * if one did (the results of the scans since the last query are then not to
+ * be trusted; later scans may also leave their waits early until the word is
+ * cleared).  It allocates nothing.  Call it outside any stream capture. */
+MGPU_API mgpu_status_t mgpu_scan_noalloc_status(void* stream);
+
+/* Self test of that status path: enqueues on `stream` a kernel whose bounded
+ * wait on a flag that nothing sets gives up after `limit` polls (1 ..
+ * 2^22) and records the timeout where a scan look-back would; the next
+ * mgpu_scan_noalloc_status() returns MGPU_ERR_LOOKBACK_TIMEOUT. */
+MGPU_API mgpu_status_t mgpu_selftest_scan_noalloc_wait(void* stream, int limit);
+
 /* ---- reduce (cta_reduce_t, common/cta_scan.hxx:9-59, as a device-wide
  * primitive).  Writes init (+) all inputs to the device pointer `out`. */
 MGPU_API mgpu_status_t mgpu_reduce(mgpu_context_t* ctx, mgpu_dtype_t type, mgpu_op_t op,

@@ -15,15 +15,20 @@
 // MGPU_SCAN_NOALLOC_MAX_COUNT elements: 65,538 words = 512 KiB + 16 bytes.
 // Every GPU that loads this library holds that array until the process exits.
 // All calls share it, and it keeps the last call's contents: each call clears
-// the counter, the error word and the status words it will use before its
-// kernel runs.  Calls whose work overlaps on the GPU (different streams, or
-// different host threads, on the same device) race on the array; callers must
-// order them, for example by issuing them on one stream.
+// the tile counter and the status words it will use before its kernel runs.
+// The error word is not cleared by a scan: a bounded look-back wait that gave
+// up stays recorded until mgpu_scan_noalloc_status() reads and clears it.
+// Calls whose work overlaps on the GPU (different streams, or different host
+// threads, on the same device) race on the array; callers must order them,
+// for example by issuing them on one stream.
 //
 // The array's host-side name is only a stand-in, not a device address; the
 // device address comes from cudaGetSymbolAddress, called once per device with
-// that device current, the first time this entry point runs on it.  Make that
-// first call outside any stream capture.
+// that device current, the first time this entry point (or the status query)
+// runs on it.  Make that first call outside any stream capture.  The address
+// is kept for the life of the process, so cudaDeviceReset() on a device after
+// its first call here is not supported: the module may be loaded again at
+// another address.
 #include "mgpu_gb300.h"
 #include "mgpu/device/scan.cuh"
 
@@ -70,7 +75,9 @@ mgpu_status_t launch(cudaStream_t stream, mgpu_scan_type_t scan_type, const void
     return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
   }
   const int64_t num_tiles = div_up(count, kTile);
-  if(cudaMemsetAsync(scratch, 0, sizeof(uint64_t) * (2 + num_tiles), stream) != cudaSuccess)
+  // Word 1 (the error word) keeps what earlier calls recorded.
+  if(cudaMemsetAsync(scratch, 0, sizeof(uint64_t), stream) != cudaSuccess ||
+     cudaMemsetAsync(scratch + 2, 0, sizeof(uint64_t) * num_tiles, stream) != cudaSuccess)
     return MGPU_ERR_CUDA;
   tile_status_t<T> status;
   status.bind(scratch + 2, num_tiles);
@@ -97,7 +104,52 @@ mgpu_status_t by_op(mgpu_op_t op, cudaStream_t s, mgpu_scan_type_t st, const voi
   return MGPU_ERR_INVALID_ARG;
 }
 
+// Self test of the status path: a bounded wait on a flag that nothing sets
+// gives up after `limit` polls and records the timeout in the scan's error
+// word, exactly as a scan look-back that gave up would.
+__device__ uint32_t g_noalloc_never_set = 0;
+
+__global__ void noalloc_wait_probe(int limit, int* error) {
+  int spins = 0;
+  while(ld_relaxed(&g_noalloc_never_set) == 0) {
+    if(++spins >= limit) {
+      raise_error(error, err_lookback_timeout);
+      break;
+    }
+    __nanosleep(64);
+  }
+}
+
 }  // namespace
+
+extern "C" mgpu_status_t mgpu_scan_noalloc_status(void* stream) {
+  int device = 0;
+  if(cudaGetDevice(&device) != cudaSuccess) return MGPU_ERR_CUDA;
+  if(device < 0 || device >= kMaxDevices) return MGPU_ERR_UNSUPPORTED;
+  uint64_t* scratch = nullptr;
+  if(scratch_address(device, &scratch) != cudaSuccess) return MGPU_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  int word = 0;
+  if(cudaMemcpyAsync(&word, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+     cudaStreamSynchronize(s) != cudaSuccess)
+    return MGPU_ERR_CUDA;
+  if(word == 0) return MGPU_OK;
+  if(cudaMemsetAsync(scratch + 1, 0, sizeof(uint64_t), s) != cudaSuccess ||
+     cudaStreamSynchronize(s) != cudaSuccess)
+    return MGPU_ERR_CUDA;
+  return word == err_lookback_timeout ? MGPU_ERR_LOOKBACK_TIMEOUT : MGPU_ERR_CUDA;
+}
+
+extern "C" mgpu_status_t mgpu_selftest_scan_noalloc_wait(void* stream, int limit) {
+  if(limit < 1 || limit > spin_limit) return MGPU_ERR_INVALID_ARG;
+  int device = 0;
+  if(cudaGetDevice(&device) != cudaSuccess) return MGPU_ERR_CUDA;
+  if(device < 0 || device >= kMaxDevices) return MGPU_ERR_UNSUPPORTED;
+  uint64_t* scratch = nullptr;
+  if(scratch_address(device, &scratch) != cudaSuccess) return MGPU_ERR_CUDA;
+  noalloc_wait_probe<<<1, 1, 0, (cudaStream_t)stream>>>(limit, (int*)(scratch + 1));
+  return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+}
 
 extern "C" mgpu_status_t mgpu_scan_noalloc(void* stream, mgpu_dtype_t type,
   mgpu_scan_type_t scan_type, mgpu_op_t op, const void* in, void* out, int64_t count,

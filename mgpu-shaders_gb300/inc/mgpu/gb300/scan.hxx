@@ -10,7 +10,9 @@
 // `op` must be associative and commutative with an identity() (plus_t,
 // maximum_t, minimum_t): a tile's aggregate folds each thread's elements
 // before the warps' partials, not in element order.  Float sums therefore
-// round differently from a sequential sum (within the usual bound).
+// round differently from a sequential sum (within the usual bound).  The
+// requirement is checked at compile time through commutative_op<op_t>, so an
+// operator that does not commute fails to build instead of scanning wrongly.
 #pragma once
 
 #include "context.hxx"
@@ -25,6 +27,15 @@ template<typename T> using plus_t = device::plus_t<T>;
 template<typename T> using maximum_t = device::max_t<T>;
 template<typename T> using minimum_t = device::min_t<T>;
 
+// Operators the scans and reductions may combine out of element order.  The
+// built-in plus, maximum and minimum commute; a caller's own operator that is
+// associative and commutative (and has a static identity()) opts in with
+//   template<> struct mgpu::gb300::commutative_op<my_op> : std::true_type {};
+template<typename op_t> struct commutative_op : std::false_type {};
+template<typename T> struct commutative_op<device::plus_t<T>> : std::true_type {};
+template<typename T> struct commutative_op<device::max_t<T>> : std::true_type {};
+template<typename T> struct commutative_op<device::min_t<T>> : std::true_type {};
+
 // Launch shapes: threads, elements per thread, persistent (1: resident CTAs
 // looping over tiles with a deferred look-back, scan_defer_kernel; 0: one
 // tile per CTA, scan_kernel), CTAs per SM asked of the compiler.
@@ -38,6 +49,9 @@ template<scan_type_t scan_type = scan_type_exc,
 status_t scan(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
   T* out, T init = op_t::identity(), op_t op = op_t(), T* reduction = nullptr) {
   using namespace device;
+  static_assert(commutative_op<op_t>::value,
+    "scan combines partials out of element order: op must be associative and commutative "
+    "(specialise mgpu::gb300::commutative_op for a user operator that is)");
   constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
   constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
   constexpr int PERSISTENT = persistent >= 0 ? persistent : (int)scan_tuning<sizeof(T)>::persistent;
@@ -116,6 +130,9 @@ template<int nt = 0, int vt = 0, typename T, typename op_t = plus_t<T>>
 status_t reduce(void* aux_data, size_t* aux_size, context_t& ctx, const T* in, int64_t count,
   T* out, T init = op_t::identity(), op_t op = op_t()) {
   using namespace device;
+  static_assert(commutative_op<op_t>::value,
+    "reduce combines partials out of element order: op must be associative and commutative "
+    "(specialise mgpu::gb300::commutative_op for a user operator that is)");
   constexpr int NT = nt ? nt : (int)scan_tuning<sizeof(T)>::nt;
   constexpr int VT = vt ? vt : (int)scan_tuning<sizeof(T)>::vt;
   constexpr int tile = NT * VT;

@@ -139,6 +139,9 @@ status_t segmented_scan(void* aux_data, size_t* aux_size, context_t& ctx, const 
   int64_t count, T* out, const int64_t* offsets, int64_t num_segments,
   T init = op_t::identity(), op_t op = op_t()) {
   using namespace device;
+  static_assert(commutative_op<op_t>::value,
+    "segmented_scan combines partials out of element order: op must be associative and "
+    "commutative (specialise mgpu::gb300::commutative_op for a user operator that is)");
   // 8192-element tiles at 3 CTAs/SM for 4-byte values (measured against 4
   // CTAs/SM and 4096-element tiles); 8-byte values spill above 2 CTAs/SM.
   constexpr int NT = 256;

@@ -46,3 +46,20 @@ def keys(rng, n, dtype, dist="uniform"):
         _ = ib
         return x
     raise ValueError(dist)
+
+
+def wide_keys(rng, n, kind):
+    """Keys of the 2^27-key radix configurations: "u64" uniform 64-bit;
+    "f32bits" uniform 32-bit patterns with the non-finite ones' exponent
+    cleared (finite floats of every magnitude); "f32normal" N(0,1) floats."""
+    if kind == "u64":
+        return rng.integers(0, 2 ** 63, n, dtype=np.uint64) * 2 + \
+            rng.integers(0, 2, n, dtype=np.uint64)
+    if kind == "f32bits":
+        raw = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+        bad = (raw & 0x7F800000) == 0x7F800000
+        raw[bad] &= np.uint32(0x807FFFFF)
+        return raw.view(np.float32)
+    if kind == "f32normal":
+        return rng.standard_normal(n).astype(np.float32)
+    raise ValueError(kind)

@@ -6,8 +6,6 @@ import subprocess
 
 import pytest
 
-pytestmark = pytest.mark.gpu
-
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 
@@ -23,6 +21,7 @@ def build_example(tmp_path):
     return exe
 
 
+@pytest.mark.gpu
 def test_cpp_template_api(tmp_path):
     import torch
     if not torch.cuda.is_available():
@@ -33,3 +32,37 @@ def test_cpp_template_api(tmp_path):
     for name in ["launch_transform", "mergesort_user_comparator", "merge_keys",
                  "scan_exclusive_in_place", "radix_sort_keys"]:
         assert "ok " + name in r.stdout
+
+
+NONCOMMUTATIVE = r"""
+#include "mgpu/gb300/scan.hxx"
+struct first_t {   // keeps its left operand: associative, not commutative
+  static __host__ __device__ int identity() { return 0; }
+  __device__ int operator()(int a, int) const { return a; }
+};
+#ifdef OPT_IN
+template<> struct mgpu::gb300::commutative_op<first_t> : std::true_type {};
+#endif
+mgpu::gb300::status_t f(mgpu::gb300::context_t& ctx, int* d, int64_t n) {
+  return mgpu::gb300::scan(ctx, d, n, d, 0, first_t());
+}
+"""
+
+
+def test_scan_rejects_an_operator_not_declared_commutative(tmp_path):
+    """The scans combine partials out of element order, so an operator must
+    be declared commutative (the built-ins are); an undeclared one is a
+    compile-time error instead of a wrong result.  Compiles only (no GPU)."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("no nvcc")
+    src = tmp_path / "op.cu"
+    src.write_text(NONCOMMUTATIVE)
+    base = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17",
+            "--extended-lambda", "-I", os.path.join(REPO, "include"),
+            "-I", os.path.join(REPO, "mgpu-shaders_gb300", "inc"), "-c", str(src),
+            "-o", str(tmp_path / "op.o")]
+    r = subprocess.run(base, capture_output=True, text=True)
+    assert r.returncode != 0 and "commutative" in r.stdout + r.stderr
+    r = subprocess.run(base[:1] + ["-DOPT_IN"] + base[1:], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

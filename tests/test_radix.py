@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from datagen import keys as gen_keys
+from datagen import wide_keys
 
 pytestmark = pytest.mark.gpu
 
@@ -155,6 +156,28 @@ def test_radix_full_size_properties(mgpu, ctx, dist):
     assert seen.all()
     eq = gk[1:] == gk[:-1]
     assert np.all(gv[1:][eq] > gv[:-1][eq])
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("kind", ["u64", "f32bits", "f32normal"])
+def test_radix_wide_full_size_exact(mgpu, ctx, oracle, kind):
+    """The 2^27-key configurations with int32 values = index: u64 uniform
+    64-bit keys, and f32 keys as uniform finite bit patterns and as N(0,1);
+    bit-exact against the oracle's parallel stable sort by radix bits."""
+    n = 1 << 27
+    # The benchmark's generator and seeds (bench.py wl_radix_wide).
+    rng = np.random.default_rng(0x6D677075 + 2 + (6 if kind == "u64" else 7))
+    k = wide_keys(rng, n, kind)
+    v = np.arange(n, dtype=np.int32)
+    dk = mgpu.DeviceArray.from_numpy(k)
+    dv = mgpu.DeviceArray.from_numpy(v)
+    ctx.radix_sort(dk, dv)
+    ctx.synchronize()
+    gk, gv = dk.numpy(), dv.numpy()
+    del dk, dv
+    ok, ov = oracle.sort_parallel(k, v, mode="radix")
+    assert np.array_equal(bits(gk), bits(ok))
+    assert np.array_equal(gv, ov)
 
 
 def test_radix_orders_with_torch_stream(mgpu, ctx, oracle, rng):

@@ -120,3 +120,18 @@ def test_segsort_full_batch(mgpu, ctx, oracle):
     gk, gv = run_segsort(mgpu, ctx, k, v, off)
     ok, ov = oracle.segmented_sort(k, v, off, mode="radix")
     assert np.array_equal(gk, ok) and np.array_equal(gv, ov)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("scan_type", ["inc", "exc"])
+def test_segscan_full_batch(mgpu, ctx, oracle, scan_type):
+    """The segmented-scan configuration: the 100,000 lognormal segments
+    (median 256, sigma 2, clipped [1, 2^20]) over int32 U[0,100) values,
+    plus; exact against per-segment scans on the host."""
+    rng = np.random.default_rng(0x6D677075 + 2 + 8)     # the benchmark's seed
+    off = lognormal_offsets(rng, 100_000)
+    n = int(off[-1])
+    x = rng.integers(0, 100, n).astype(np.int32)
+    got = run_segscan(mgpu, ctx, x, off, scan_type)
+    ref = oracle.segmented_scan_int(x, off, exclusive=scan_type == "exc")
+    assert np.array_equal(got, ref)
