@@ -12,11 +12,12 @@ mgpu_status_t radix_sort_w64(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
     auto go = [&](auto* vp) -> mgpu_status_t {
       typedef std::remove_pointer_t<decltype(vp)> V;
       if(d_count)   // count read on the device: the default shape
-        return radix_sort_kv<256, 12, 3, true>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+        return radix_sort_kv<256, 16, 3, true>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           d_count);
       switch(variant) {
-        case 1: return radix_sort_kv<256, 8, 4>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
-        default: return radix_sort_kv<256, 12, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
+        case 1: return radix_sort_kv<256, 12, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
+        case 2: return radix_sort_kv<384, 10, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
+        default: return radix_sort_kv<256, 16, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
       }
     };
     if(val_bytes == 0) return go((no_values*)nullptr);

@@ -12,16 +12,21 @@
 //  * radix_histogram: every digit place's 256-bin histogram from a single
 //    read of the keys (4 B/key instead of one upsweep read per digit).
 //  * onesweep_pass: one launch per digit.  Each CTA takes the next tile id
-//    from an atomic counter (so every predecessor tile is already resident),
-//    bulk-copies its keys and values into shared memory with the TMA engine,
-//    ranks digits per warp (peer lanes found with one ballot per digit bit;
-//    stable: rows of 32 lanes in element order), publishes its per-digit
-//    counts, then walks back over predecessor tiles' published counts
-//    (decoupled look-back, several predecessors per L2 round trip, the first
-//    round overlapping the shared-memory scatter) to find its global offset
-//    per digit.  Keys and values are scattered to shared memory in local digit
-//    order and written out in runs, so global stores coalesce.  Per pass the
-//    kernel reads and writes each key and value once.
+//    from an atomic counter (so every predecessor tile is already resident)
+//    and bulk-copies the tile's keys into shared memory with the TMA engine.
+//    The kernel is bound by shared-memory traffic and by how many warps and
+//    keys each SM holds, so it keeps almost nothing per key in registers:
+//    keys are read from the staged tile each time they are needed and ranks
+//    are packed 16-bit pairs.  Each warp ranks its rows of 32 keys (stable,
+//    element order) through one 64-bit mask+count word per digit; the CTA
+//    publishes its per-digit counts and walks back over predecessor tiles'
+//    published counts (decoupled look-back, several predecessors per L2 round
+//    trip, overlapping the scatter) to find its global offset per digit.
+//    Keys are scattered into a second shared-memory region in local digit
+//    order and written out in runs, so global stores coalesce; the values'
+//    bulk copy reuses the first region once the keys have left it, and the
+//    values follow the same permutation.  Per pass the kernel reads and
+//    writes each key and value once.
 //
 // The look-back status of (tile, digit) is one 32-bit word: two flag bits
 // (aggregate / inclusive prefix) over a 30-bit count, hence count < 2^30.
@@ -62,31 +67,39 @@ struct onesweep_args {
   const int64_t* count_ptr = nullptr;
 };
 
+// Shared memory of one onesweep tile of NT threads x ITEMS keys:
+//   A  the staged tile: keys (raw on the first pass), later the values; 16
+//      spare bytes take the aligned window of a tile that does not start on
+//      16 bytes;
+//   B  the warps' match words while ranking (2 KB per warp), then the keys
+//      in local digit order, then the values in that order;
+//   W  each warp's digit offsets within the tile, then one digit byte per
+//      sorted position (the values' write-out needs the digits after the
+//      sorted keys have left B);
+//   plus the digits' global bases, scan scratch, the mbarrier and the tile id.
 template<typename K, typename V, int NT, int ITEMS>
 struct onesweep_layout {
   typedef typename radix_key<K>::bits_t U;
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
   static constexpr int tile = NT * ITEMS;
   static constexpr int num_warps = NT / 32;
-  // The key and value buffers carry 16 spare bytes: a tile that does not
-  // start on 16 bytes is bulk-copied as the aligned window around it.
-  static constexpr size_t keys_off = 0;
-  static constexpr size_t vals_off = keys_off + sizeof(U) * tile + 16;
-  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile + 16 : 0);
-  static constexpr size_t gbase_off = hist_off + sizeof(uint32_t) * num_warps * radix_bins;
+  static constexpr size_t elem = has_values && sizeof(V) > sizeof(U) ? sizeof(V) : sizeof(U);
+  static constexpr size_t a_off = 0;
+  static constexpr size_t b_off = a_off + elem * tile + 16;
+  static constexpr size_t w_off = b_off + elem * tile;
+  static constexpr size_t w_bytes =
+    ((size_t)num_warps * radix_bins * 4 > (size_t)tile ? (size_t)num_warps * radix_bins * 4
+                                                        : (size_t)tile + 15) & ~(size_t)15;
+  static constexpr size_t gbase_off = w_off + w_bytes;
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
   static constexpr size_t tile_off = bar_off + sizeof(uint64_t) * 2;
   static constexpr size_t bytes = tile_off + 16;
-  // Each warp's slice of the key buffer (32 * ITEMS keys) doubles as its two
-  // banks of 256 match masks while it ranks, when it is large enough.
-  static constexpr bool match_in_slice = sizeof(U) * 32 * ITEMS >= 2 * 256 * sizeof(uint32_t);
-  // A window copy shifts the staged keys by up to 16 bytes, and the ranking
-  // words by as much; they must still end before the next warp's keys.
-  static constexpr bool window_ok =
-    !match_in_slice || sizeof(U) * 32 * ITEMS >= 2 * 256 * sizeof(uint32_t) + 16;
   static_assert(NT >= radix_bins && NT % 32 == 0, "one thread per digit");
   static_assert((sizeof(U) * tile) % 16 == 0, "bulk-copy granularity");
+  static_assert(elem * tile >= (size_t)num_warps * 2 * radix_bins * 4,
+    "the warps' match words fit in region B");
+  static_assert(ITEMS % 2 == 0 && tile <= 65536, "ranks are packed 16-bit pairs");
 };
 
 // Exclusive scan of two 256-entry arrays held by threads 0..255 (one digit
@@ -167,46 +180,26 @@ struct onesweep_tile_t {
   int64_t out_base;        // absolute index of the sort's first element
 };
 
-// Claims the next tile id and prepares shared memory (barrier, counters).
-// Returns the tile id; every thread of the CTA must call it.
+// Claims the next tile id and initialises the tile's mbarrier.  Returns the
+// tile id; every thread of the CTA must call it.
 template<typename K, typename V, int NT, int ITEMS>
 __device__ __forceinline__ int onesweep_begin(uint32_t* tile_counter, unsigned char* smem) {
   typedef onesweep_layout<K, V, NT, ITEMS> L;
-  uint32_t* whist = (uint32_t*)(smem + L::hist_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
   int* s_tile = (int*)(smem + L::tile_off);
-  const int tid = threadIdx.x;
-  if(tid == 0) {
+  if(threadIdx.x == 0) {
     *s_tile = (int)atomicAdd(tile_counter, 1u);
     mbar_init(bar, 1);
     fence_mbar_init();
   }
-  // The ballot path counts digits in the warp histograms directly; the match
-  // path keeps its counts in the warps' key slices and writes whist whole.
-  if(!L::match_in_slice)
-    for(int i = tid; i < L::num_warps * radix_bins; i += NT) whist[i] = 0;
   __syncthreads();
   return *s_tile;
 }
 
-// Peers of this lane in the warp (lanes whose 8-bit digit equals its own),
-// found with one ballot per digit bit, as the reference's get_matching_lanes
-// (common/cta_radix.hxx:242-256) does; used where no shared-memory match
-// masks fit.  The digit sits at bit offset `shift` of the key; the key's bits
-// are tested against per-pass masks (bit_mask[b] = 1 << (shift + b)): `same`
-// collects lanes that share this lane's set bits, `diff` lanes that set one
-// of its clear bits.
-template<typename U>
-__device__ __forceinline__ uint32_t match_key_digit8(U k, const U (&bit_mask)[8]) {
-  uint32_t same = 0xffffffffu, diff = 0;
-#pragma unroll
-  for(int b = 0; b < 8; ++b) {
-    const bool bit = (k & bit_mask[b]) != 0;
-    const uint32_t v = __ballot_sync(0xffffffffu, bit);
-    if(bit) same &= v;
-    else diff |= v;
-  }
-  return same & ~diff;
+// Orders this thread's earlier generic-proxy accesses to shared memory
+// before its later bulk copies (async proxy) into the same bytes.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Decoupled look-back of one digit: the sum of the counts of all predecessor
@@ -281,10 +274,12 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   constexpr int TILE = L::tile;
   constexpr int NWARPS = L::num_warps;
   constexpr bool HAS_V = L::has_values;
+  constexpr int CHUNK = 4;                  // write-out: loads in flight per thread
 
-  U* ks = (U*)(smem + L::keys_off);
-  V* vs = (V*)(smem + L::vals_off);
-  uint32_t* whist = (uint32_t*)(smem + L::hist_off);
+  unsigned char* A = smem + L::a_off;
+  unsigned char* B = smem + L::b_off;
+  uint32_t* W = (uint32_t*)(smem + L::w_off);
+  uint8_t* Wb = (uint8_t*)(smem + L::w_off);
   int* gbase = (int*)(smem + L::gbase_off);
   uint32_t* stmp = (uint32_t*)(smem + L::scan_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
@@ -307,8 +302,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     vstart = base & ~(VV - 1);
     kend = (base + TILE + KV - 1) & ~(KV - 1);
     vend = (base + TILE + VV - 1) & ~(VV - 1);
-    bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count) &&
-      (L::window_ok || (kstart == base && vstart == base));
+    bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count);
   } else {
     bulk = a.tma && valid == TILE && 0 == (base & (KV - 1)) && 0 == (base & (VV - 1));
   }
@@ -317,20 +311,24 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 
   if(bulk && tid == 0) {
     const uint32_t kbytes = (uint32_t)(sizeof(U) * (kend - kstart));
-    const uint32_t vbytes = HAS_V ? (uint32_t)(sizeof(V) * (vend - vstart)) : 0u;
-    mbar_arrive_expect_tx(bar, kbytes + vbytes);
-    bulk_load(ks, a.keys_in + kstart, kbytes, bar);
-    if(HAS_V) bulk_load(vs, a.vals_in + vstart, vbytes, bar);
+    mbar_arrive_expect_tx(bar, kbytes);
+    bulk_load(A, a.keys_in + kstart, kbytes, bar);
   }
+
+  // This warp's match words: one 64-bit word per digit, at the start of B.
+  uint32_t* mw = (uint32_t*)B + warp * 2 * radix_bins;
+  for(int j = lane; j < 2 * radix_bins / 4; j += 32)
+    reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
 
   // Concentration of this pass's digits: when some digit holds more than
   // 1/128 of the keys, rows of 32 equal digits become likely (equal keys sit
   // together after earlier passes) and the ranking checks for them.  Warp
   // maxima and sums of the digit totals go to scan scratch words 16..31.
+  uint32_t hval = 0;
   if(tid < radix_bins) {
-    const uint32_t h = t.hist[tid];
-    const uint32_t m = __reduce_max_sync(0xffffffffu, h);
-    const uint32_t sum = __reduce_add_sync(0xffffffffu, h);
+    hval = t.hist[tid];
+    const uint32_t m = __reduce_max_sync(0xffffffffu, hval);
+    const uint32_t sum = __reduce_add_sync(0xffffffffu, hval);
     if(lane == 0) { stmp[16 + warp] = m; stmp[24 + warp] = sum; }
   }
 
@@ -338,7 +336,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   // e = warp_base + 32 * i + lane; it is in range while 32 * i < rem.
   const int warp_base = warp * 32 * ITEMS;
   const int rem = valid - warp_base - lane;
-  U k[ITEMS];
+  U* const ak = (U*)A + koff + warp_base + lane;        // this thread's staged keys
   if(bulk) {
     // Only warp 0 polls the barrier; the other warps sleep at the CTA
     // barrier below instead of spending issue slots.  The mbarrier phase
@@ -352,13 +350,18 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
       return;
     }
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) k[i] = ks[koff + warp_base + 32 * i + lane];
   } else {
-    __syncthreads();
+    // Plain loads; positions past the tile's end take the largest radix
+    // bits, so they rank last (after every real key with digit 255).
+    U fill = ~(U)0;
+    if(a.first) {
+      const K k = radix_key<K>::from_bits(~(U)0);
+      memcpy(&fill, &k, sizeof(U));
+    }
     const U* src = a.keys_in + base + warp_base + lane;
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) k[i] = 32 * i < rem ? src[32 * i] : ~(U)0;
+#pragma unroll 4
+    for(int i = 0; i < ITEMS; ++i) ak[32 * i] = 32 * i < rem ? src[32 * i] : fill;
+    __syncthreads();
   }
   bool check_uniform;
   {
@@ -367,51 +370,35 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     for(int w = 0; w < radix_bins / 32; ++w) { mx = max(mx, stmp[16 + w]); total += stmp[24 + w]; }
     check_uniform = (uint64_t)mx * 128 > total;
   }
-  if(a.first) {
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) {
-      if(32 * i < rem) {
-        K key;
-        memcpy(&key, &k[i], sizeof(K));
-        k[i] = radix_key<K>::to_bits(key);
-      }
+  // Radix bits of item i (the staged copy holds raw keys on the first pass).
+  auto key_bits = [&](int i) -> U {
+    U u = ak[32 * i];
+    if(a.first) {
+      K key;
+      memcpy(&key, &u, sizeof(K));
+      u = radix_key<K>::to_bits(key);
     }
-  }
+    return u;
+  };
 
   // Warp-level stable ranking: item i of every lane forms one row; lanes
-  // holding equal digits are peers.  The rank counts earlier rows and lower
-  // lanes of the same row (element order), via a per-warp digit counter.
-  uint32_t r[ITEMS];
-  uint32_t* wh = whist + warp * radix_bins;
-  const uint32_t lt_mask = lanemask_lt();
-  // Each warp's ranking words start `moff` elements into its slice: at or
-  // after the end of the previous warp's staged keys (which that warp may
-  // still be reading) and on 16 bytes (they are cleared with 16-byte stores).
-  const int moff = (int)((koff + KV - 1) & ~(KV - 1));
-  // Where warp w's count of digit d sits after ranking.
-  auto warp_count = [&](int w, int d) -> uint32_t {
-    if constexpr(L::match_in_slice)
-      return ((const uint32_t*)(ks + moff + w * 32 * ITEMS))[2 * d + 1 - ((d >> 4) & 1)];
-    else return whist[w * radix_bins + d];
-  };
-  if constexpr(L::match_in_slice) {
-    // Per digit, one 64-bit word in this warp's slice of the key buffer (its
-    // keys are already in registers): one half collects the row's peer mask
-    // (every lane ORs its lane bit in), the other is the warp's running
-    // count.  A lane reads both halves in one load; the lowest peer writes
-    // back the advanced count with a clear mask.  Three shared-memory
-    // operations per key.  Digits with bit 4 set keep their mask in the upper
-    // half, so the masks of any 32 digits spread over all 32 banks.
-    uint32_t* mw = (uint32_t*)(ks + moff + warp_base);
-    __syncwarp();
-    for(int j = lane; j < 2 * radix_bins / 4; j += 32)
-      reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
-    __syncwarp();
+  // holding equal digits are peers.  Per digit, one 64-bit word: one half
+  // collects the row's peer mask (every lane ORs its lane bit in), the
+  // other is the warp's running count.  A lane reads both halves in one
+  // load; the lowest peer writes back the advanced count with a clear mask.
+  // Three shared-memory operations per key.  Digits with bit 4 set keep their
+  // mask in the upper half, so the masks of any 32 digits spread over all 32
+  // banks.  The rank counts earlier rows and lower lanes of the same row
+  // (element order).  Ranks (< 2^16) are kept as packed pairs.
+  uint32_t rp[ITEMS / 2];
+  {
+    const uint32_t lt_mask = lanemask_lt();
     const uint32_t lane_bit = 1u << lane;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
-      const uint32_t d = extract_digit(k[i], a.shift, 8);
+      const uint32_t d = extract_digit(key_bits(i), a.shift, 8);
       const uint32_t hi = (d >> 4) & 1;            // mask in the upper half
+      uint32_t rank;
       if(check_uniform && __all_sync(0xffffffffu, d == __shfl_sync(0xffffffffu, d, 0))) {
         // One digit across the row (common once equal keys sit together):
         // the peers are the whole warp, and same-address atomics are skipped.
@@ -420,37 +407,23 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
         __syncwarp();
         if(lane == 0) *cw = cnt + 32;
         __syncwarp();
-        r[i] = cnt + lane;
-        continue;
+        rank = cnt + lane;
+      } else {
+        atomicOr(&mw[2 * d + hi], lane_bit);
+        __syncwarp();
+        const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
+        __syncwarp();
+        const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
+        const uint32_t below = peers & lt_mask;
+        if(!below) {
+          const uint32_t next = cnt + __popc(peers);
+          *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
+        }
+        __syncwarp();
+        rank = cnt + __popc(below);
       }
-      atomicOr(&mw[2 * d + hi], lane_bit);
-      __syncwarp();
-      const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
-      __syncwarp();
-      const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
-      const uint32_t below = peers & lt_mask;
-      if(!below) {
-        const uint32_t next = cnt + __popc(peers);
-        *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
-      }
-      __syncwarp();
-      r[i] = cnt + __popc(below);
-    }
-  } else {
-    // Peers through one ballot per digit bit.
-    U bit_mask[8];
-#pragma unroll
-    for(int b = 0; b < 8; ++b) bit_mask[b] = (U)1 << (a.shift + b);
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) {
-      const uint32_t d = extract_digit(k[i], a.shift, 8);
-      const uint32_t peers = match_key_digit8(k[i], bit_mask);
-      const uint32_t cnt = wh[d];
-      __syncwarp();
-      const uint32_t below = peers & lt_mask;
-      if(!below) wh[d] = cnt + __popc(peers);
-      __syncwarp();
-      r[i] = cnt + __popc(below);
+      if(i & 1) rp[i >> 1] |= rank << 16;
+      else rp[i >> 1] = rank;
     }
   }
   __syncthreads();
@@ -458,53 +431,52 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   // Digit `tid`: counts per warp -> exclusive offsets over warps (kept in
   // registers); publish the tile's count (inclusive for tile 0) before
   // scanning, so successors can proceed as early as possible.
-  uint32_t tile_cnt = 0, glob_cnt = 0, valid_cnt = 0;
+  uint32_t tile_cnt = 0, valid_cnt = 0;
   uint32_t wexcl[NWARPS];
   if(tid < radix_bins) {
+    const uint32_t hi = (tid >> 4) & 1;
 #pragma unroll
     for(int w = 0; w < NWARPS; ++w) {
-      const uint32_t c = warp_count(w, tid);
+      const uint32_t c = ((const uint32_t*)B)[w * 2 * radix_bins + 2 * tid + 1 - hi];
       wexcl[w] = tile_cnt;
       tile_cnt += c;
     }
     valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
     st_relaxed(&t.lb_row[tid], (tile ? lb_agg : lb_inc) | valid_cnt);
-    glob_cnt = t.hist[tid];
   }
-  uint32_t tile_start = tile_cnt, glob_start = glob_cnt;
+  uint32_t tile_start = tile_cnt, glob_start = hval;
   scan_256_pair(tile_start, glob_start, stmp);
 
   // Issue the first look-back window now; its L2 round trip overlaps the
-  // shared-memory scatter below.
+  // key scatter below.
   lookback_window_t<WINDOW> lbw;
   if(tid < radix_bins) {
     if(tile > 0) lbw.issue(t.lb_row + tid - radix_bins, tile);
 #pragma unroll
-    for(int w = 0; w < NWARPS; ++w) whist[w * radix_bins + tid] = wexcl[w] + tile_start;
+    for(int w = 0; w < NWARPS; ++w) W[w * radix_bins + tid] = wexcl[w] + tile_start;
   }
   __syncthreads();
 
-  // Local positions; scatter keys (and values) into shared memory in digit
-  // order.  All reads of the staged keys happened before the barriers above.
+  // Keys into B in local digit order; the ranks become local positions.
+  {
+    const uint32_t* wh = W + warp * radix_bins;
 #pragma unroll
-  for(int i = 0; i < ITEMS; ++i) {
-    uint32_t d = extract_digit(k[i], a.shift, 8);
-    r[i] += wh[d];
-    ks[r[i]] = k[i];
-  }
-  if constexpr(HAS_V) {
-    V v[ITEMS];
-    if(bulk) {
-#pragma unroll
-      for(int i = 0; i < ITEMS; ++i) v[i] = vs[voff + warp_base + 32 * i + lane];
-    } else {
-      const V* src = a.vals_in + base + warp_base + lane;
-#pragma unroll
-      for(int i = 0; i < ITEMS; ++i) v[i] = 32 * i < rem ? src[32 * i] : V();
+    for(int i = 0; i < ITEMS; ++i) {
+      const U k = key_bits(i);
+      const uint32_t sh = (i & 1) * 16;
+      const uint32_t r = ((rp[i >> 1] >> sh) & 0xffffu) + wh[extract_digit(k, a.shift, 8)];
+      rp[i >> 1] = (rp[i >> 1] & ~(0xffffu << sh)) | (r << sh);
+      ((U*)B)[r] = k;
     }
-    __syncthreads();
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) vs[r[i]] = v[i];
+  }
+  __syncthreads();
+  // A is free: the values' bulk copy overlaps the look-back and the key
+  // write-out.
+  if(HAS_V && bulk && tid == 0) {
+    const uint32_t vbytes = (uint32_t)(sizeof(V) * (vend - vstart));
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, vbytes);
+    bulk_load(A, a.vals_in + vstart, vbytes, bar);
   }
 
   // Finish the look-back, publish the inclusive prefix, and form each
@@ -520,38 +492,76 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   __syncthreads();
 
   // Write out in local order: consecutive threads hit consecutive addresses
-  // inside each digit's run.  Loads first, then stores, for memory-level
-  // parallelism.
-  const int out_rem = valid - tid;
+  // inside each digit's run.  CHUNK loads, then CHUNK stores.  Each
+  // position's digit is kept (W is free now) for the values.
   U* keys_out = a.keys_out + t.out_base;
-  V* vals_out = a.vals_out + t.out_base;
-  U u[ITEMS];
-  uint32_t dst[ITEMS];
 #pragma unroll
-  for(int j = 0; j < ITEMS; ++j) {
-    int idx = j * NT + tid;
-    u[j] = j * NT < out_rem ? ks[idx] : 0;
-    dst[j] = (uint32_t)gbase[extract_digit(u[j], a.shift, 8)] + idx;
-  }
+  for(int j0 = 0; j0 < ITEMS; j0 += CHUNK) {
+    U u[CHUNK];
+    uint32_t dst[CHUNK];
 #pragma unroll
-  for(int j = 0; j < ITEMS; ++j) {
-    if(j * NT < out_rem) {
-      if(a.last) {
-        K key = radix_key<K>::from_bits(u[j]);
-        // Convert in registers and store one word (a memcpy straight to
-        // global memory may be split into narrow stores).
-        U out;
-        memcpy(&out, &key, sizeof(U));
-        keys_out[dst[j]] = out;
-      } else {
-        keys_out[dst[j]] = u[j];
+    for(int c = 0; c < CHUNK; ++c) {
+      const int idx = (j0 + c) * NT + tid;
+      if(j0 + c < ITEMS && idx < valid) {
+        u[c] = ((const U*)B)[idx];
+        const uint32_t d = extract_digit(u[c], a.shift, 8);
+        if(HAS_V) Wb[idx] = (uint8_t)d;
+        dst[c] = (uint32_t)gbase[d] + idx;
+      }
+    }
+#pragma unroll
+    for(int c = 0; c < CHUNK; ++c) {
+      if(j0 + c < ITEMS && (j0 + c) * NT + tid < valid) {
+        if(a.last) {
+          K key = radix_key<K>::from_bits(u[c]);
+          // Convert in registers and store one word (a memcpy straight to
+          // global memory may be split into narrow stores).
+          U out;
+          memcpy(&out, &key, sizeof(U));
+          keys_out[dst[c]] = out;
+        } else {
+          keys_out[dst[c]] = u[c];
+        }
       }
     }
   }
   if constexpr(HAS_V) {
+    V* const av = (V*)A + voff + warp_base + lane;     // this thread's staged values
+    if(bulk) {
+      bool ok = true;
+      if(warp == 0) ok = mbar_wait_bounded(bar, 1, a.error);
+      if(__syncthreads_or(!ok)) {
+        if(warp == 0) mbar_wait_bounded(bar, 1, a.error);
+        return;
+      }
+    } else {
+      __syncthreads();                     // the sorted keys have left B
+      const V* src = a.vals_in + base + warp_base + lane;
+#pragma unroll 4
+      for(int i = 0; i < ITEMS; ++i) if(32 * i < rem) av[32 * i] = src[32 * i];
+      __syncwarp();                        // each warp reads only its own rows
+    }
 #pragma unroll
-    for(int j = 0; j < ITEMS; ++j)
-      if(j * NT < out_rem) vals_out[dst[j]] = vs[j * NT + tid];
+    for(int i = 0; i < ITEMS; ++i)
+      if(32 * i < rem) ((V*)B)[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = av[32 * i];
+    __syncthreads();
+    V* vals_out = a.vals_out + t.out_base;
+#pragma unroll
+    for(int j0 = 0; j0 < ITEMS; j0 += CHUNK) {
+      V v[CHUNK];
+      uint32_t dst[CHUNK];
+#pragma unroll
+      for(int c = 0; c < CHUNK; ++c) {
+        const int idx = (j0 + c) * NT + tid;
+        if(j0 + c < ITEMS && idx < valid) {
+          v[c] = ((const V*)B)[idx];
+          dst[c] = (uint32_t)gbase[Wb[idx]] + idx;
+        }
+      }
+#pragma unroll
+      for(int c = 0; c < CHUNK; ++c)
+        if(j0 + c < ITEMS && (j0 + c) * NT + tid < valid) vals_out[dst[c]] = v[c];
+    }
   }
 }
 

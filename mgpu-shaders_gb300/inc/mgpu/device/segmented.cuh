@@ -45,7 +45,9 @@ enum seg_counter_t {
   sc_next_cta, sc_next_warp, sc_next_slice, sc_pass_tiles /* + pass */, sc_count = sc_pass_tiles + 8
 };
 
-template<int TILE, int SLICE, int PASSES>
+// CTA_MAX: the largest segment one CTA sorts in shared memory; larger
+// segments are cut into onesweep tiles of LARGE_TILE keys.
+template<int CTA_MAX, int LARGE_TILE, int SLICE, int PASSES>
 __global__ void seg_classify(const int64_t* offsets, int64_t num_segments, seg_state_t s) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_segments; i += stride) {
@@ -56,10 +58,10 @@ __global__ void seg_classify(const int64_t* offsets, int64_t num_segments, seg_s
       s.warp_list[atomicAdd(&s.counters[sc_warp], 1u)] = (int)i;
     } else if(n <= SLICE) {
       s.slice_list[atomicAdd(&s.counters[sc_slice], 1u)] = (int)i;
-    } else if(n <= TILE) {
+    } else if(n <= CTA_MAX) {
       s.cta_list[atomicAdd(&s.counters[sc_cta], 1u)] = (int)i;
     } else {
-      int tiles = (int)div_up(n, TILE);
+      int tiles = (int)div_up(n, LARGE_TILE);
       int l = (int)atomicAdd(&s.counters[sc_large], 1u);
       int tb = (int)atomicAdd(&s.counters[sc_tiles], (uint32_t)tiles);
       s.large_seg[l] = (int)i;

@@ -22,10 +22,26 @@
 namespace mgpu {
 namespace gb300 {
 
-// Default tile shapes per key width (threads, keys per thread, CTAs per SM).
-template<int key_bytes> struct radix_tuning;
-template<> struct radix_tuning<4> { enum { nt = 256, vt = 20, min_blocks = 3 }; };
-template<> struct radix_tuning<8> { enum { nt = 256, vt = 12, min_blocks = 3 }; };
+// Default onesweep tile shapes (threads, keys per thread, CTAs per SM) by
+// the width of the staged elements (the wider of key and value): 8192-key
+// tiles for 4-byte elements, 4096 for 8-byte ones; three CTAs of 73 KB of
+// shared memory per SM either way.
+template<int elem_bytes> struct radix_tuning;
+template<> struct radix_tuning<4> { enum { nt = 256, vt = 32, min_blocks = 3 }; };
+template<> struct radix_tuning<8> { enum { nt = 256, vt = 16, min_blocks = 3 }; };
+
+template<typename K, typename V>
+constexpr int radix_elem_bytes() {
+  return (!std::is_same<V, device::no_values>::value && sizeof(V) > sizeof(K)) ? (int)sizeof(V)
+                                                                               : (int)sizeof(K);
+}
+
+// Shape of the one-CTA sort that takes arrays of at most one such tile (and
+// the segmented sort's segments of at most one tile): it holds the whole tile
+// in registers, so it keeps the smaller tile.
+template<int key_bytes> struct cta_sort_tuning;
+template<> struct cta_sort_tuning<4> { enum { nt = 256, vt = 20 }; };
+template<> struct cta_sort_tuning<8> { enum { nt = 256, vt = 12 }; };
 
 // Largest count the 30-bit look-back status word can carry.
 constexpr int64_t radix_max_count = (int64_t(1) << 30) - 1;
@@ -44,6 +60,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
   constexpr int passes = (int)sizeof(K);          // 8-bit digits
   constexpr int tile = nt * vt;
   typedef onesweep_layout<K, V, nt, vt> L;
+  constexpr int cnt = cta_sort_tuning<sizeof(K)>::nt, cvt = cta_sort_tuning<sizeof(K)>::vt;
 
   if(count < 0 || count > radix_max_count) return MGPU_ERR_INVALID_ARG;
 
@@ -52,18 +69,18 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
   // graph serves any size up to it.
   if(dev_count != (d_count != nullptr)) return MGPU_ERR_INVALID_ARG;
   int64_t num_tiles = div_up(count, tile);
-  if(num_tiles <= 1 && !d_count) {
-    // One tile: the whole sort runs in shared memory in one CTA; no aux.
+  if(count <= (int64_t)cnt * cvt && !d_count) {
+    // One CTA tile: the whole sort runs in shared memory in one CTA; no aux.
     char* unused = nullptr;
     status_t s0;
     if(resolve_aux(ctx, aux_data, aux_size, 0, unused, s0)) return s0;
     if(count <= 1) return MGPU_OK;
     if(!keys || (has_values && !vals)) return MGPU_ERR_INVALID_ARG;
-    typedef seg_small_layout<K, V, nt, vt, vt> SL;
-    auto k1 = radix_sort_cta<K, V, nt, vt, vt, passes>;
+    typedef seg_small_layout<K, V, cnt, cvt, cvt> SL;
+    auto k1 = radix_sort_cta<K, V, cnt, cvt, cvt, passes>;
     if(!ctx.allow_smem(k1, SL::bytes)) return MGPU_ERR_CUDA;
     return ctx.launch("radix_sort_cta", [&] {
-      k1<<<1, nt, SL::bytes, ctx.stream>>>(keys, vals, (int)count);
+      k1<<<1, cnt, SL::bytes, ctx.stream>>>(keys, vals, (int)count);
     });
   }
   aux_layout_t lay;
@@ -158,7 +175,7 @@ template<int nt = 0, int vt = 0, int num_bits = 8, typename K, typename V>
 status_t radix_sort(void* aux_data, size_t& aux_size, context_t& ctx, K* keys, V* vals,
   int64_t count) {
   static_assert(num_bits >= 1 && num_bits <= 8, "digit width of the reference's template");
-  constexpr int b = sizeof(K);
+  constexpr int b = radix_elem_bytes<K, V>();
   return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
     aux_data, &aux_size, ctx, keys, vals, count);
 }
@@ -172,7 +189,7 @@ status_t radix_sort(context_t& ctx, K* keys, int64_t count) {
 }
 template<typename K, typename V>
 status_t radix_sort(context_t& ctx, K* keys, V* vals, int64_t count) {
-  constexpr int b = sizeof(K);
+  constexpr int b = radix_elem_bytes<K, V>();
   return radix_sort_kv<radix_tuning<b>::nt, radix_tuning<b>::vt, radix_tuning<b>::min_blocks>(
     nullptr, nullptr, ctx, keys, vals, count);
 }

@@ -25,20 +25,27 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   int64_t count, const int64_t* offsets, int64_t num_segments) {
   using namespace device;
   typedef typename radix_key<K>::bits_t U;
-  typedef radix_tuning<sizeof(K)> T;
-  constexpr int NT = T::nt, ITEMS = T::vt, MINB = T::min_blocks;
+  // Segments of at most one CTA tile sort in the small-segment kernel; larger
+  // ones go through onesweep passes over tiles of the plain sort's shape.
+  typedef cta_sort_tuning<sizeof(K)> T;
+  constexpr int NT = T::nt, ITEMS = T::vt;
   constexpr int TILE = NT * ITEMS;
+  typedef radix_tuning<radix_elem_bytes<K, V>()> OT;
+  constexpr int ONT = OT::nt, OITEMS = OT::vt, MINB = OT::min_blocks;
+  constexpr int OTILE = ONT * OITEMS;
   constexpr int SLICE_ITEMS = ITEMS;
   constexpr int SMALL_MINB = 3;   // 3 CTAs/SM: 1.66 ms against 1.91 ms at 2 (108 registers)
   constexpr int SLICE = 32 * SLICE_ITEMS;
   constexpr int PASSES = sizeof(K);
   constexpr bool has_values = !std::is_same<V, no_values>::value;
   typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> SL;
-  typedef onesweep_layout<K, V, NT, ITEMS> OL;
+  typedef onesweep_layout<K, V, ONT, OITEMS> OL;
   if(count < 0 || num_segments < 0 || count > radix_max_count || num_segments > INT32_MAX)
     return MGPU_ERR_INVALID_ARG;
+  // Large segments hold more than TILE keys each; each adds at most one
+  // partial onesweep tile.
   const int64_t max_large = std::min<int64_t>(num_segments, count / (TILE + 1));
-  const int64_t max_tiles = max_large ? div_up(count, TILE) + max_large : 0;
+  const int64_t max_tiles = max_large ? div_up(count, OTILE) + max_large : 0;
   aux_layout_t lay;
   size_t cnt_off = lay.add(sizeof(uint32_t) * sc_count);
   size_t warp_off = lay.add(sizeof(int) * num_segments);
@@ -73,7 +80,8 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
     return MGPU_ERR_CUDA;
   int cgrid = (int)std::min<int64_t>(div_up(num_segments, 256), (int64_t)ctx.sm_count * 8);
   st = ctx.launch("seg_classify", [&] {
-    seg_classify<TILE, SLICE, PASSES><<<cgrid, 256, 0, ctx.stream>>>(offsets, num_segments, s);
+    seg_classify<TILE, OTILE, SLICE, PASSES><<<cgrid, 256, 0, ctx.stream>>>(offsets,
+      num_segments, s);
   });
   if(st) return st;
 
@@ -88,11 +96,11 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   if(st || !max_large) return st;
 
   st = ctx.launch("seg_histogram", [&] {
-    seg_histogram<K, 512, TILE, PASSES><<<ctx.sm_count * 4, 512, 0, ctx.stream>>>(keys,
+    seg_histogram<K, 512, OTILE, PASSES><<<ctx.sm_count * 4, 512, 0, ctx.stream>>>(keys,
       offsets, s);
   });
   if(st) return st;
-  auto pass_kernel = seg_onesweep_pass<K, V, NT, ITEMS, MINB, PASSES>;
+  auto pass_kernel = seg_onesweep_pass<K, V, ONT, OITEMS, MINB, PASSES>;
   if(!ctx.allow_smem(pass_kernel, OL::bytes)) return MGPU_ERR_CUDA;
   U* k_io[2] = { (U*)keys, (U*)(base + k2_off) };
   V* v_io[2] = { vals, has_values ? (V*)(base + v2_off) : nullptr };
@@ -112,7 +120,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
     a.last = p == PASSES - 1;
     a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));
     st = ctx.launch("seg_onesweep_pass", [&] {
-      pass_kernel<<<(unsigned)max_tiles, NT, OL::bytes, ctx.stream>>>(a, offsets, s, p);
+      pass_kernel<<<(unsigned)max_tiles, ONT, OL::bytes, ctx.stream>>>(a, offsets, s, p);
     });
     if(st) return st;
   }
