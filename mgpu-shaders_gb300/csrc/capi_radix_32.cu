@@ -23,11 +23,11 @@ mgpu_status_t radix_sort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
       K* k = (K*)keys;
       V* v = (V*)vals;
       if(d_count)   // count read on the device: the default shape
-        return sort_shape<256, 32, 3, true>(c, k, v, count, aux, aux_size, d_count);
+        return sort_shape<384, 20, 3, true>(c, k, v, count, aux, aux_size, d_count);
       switch(variant) {
-        case 1: return sort_shape<384, 20, 3>(c, k, v, count, aux, aux_size, nullptr);
+        case 1: return sort_shape<256, 32, 3>(c, k, v, count, aux, aux_size, nullptr);
         case 2: return sort_shape<256, 24, 3>(c, k, v, count, aux, aux_size, nullptr);
-        default: return sort_shape<256, 32, 3>(c, k, v, count, aux, aux_size, nullptr);
+        default: return sort_shape<384, 20, 3>(c, k, v, count, aux, aux_size, nullptr);
       }
     };
     if(val_bytes == 0) return go((no_values*)nullptr);

@@ -7,12 +7,12 @@
 
 namespace variants {
 
-// radix_sort onesweep tiles, all at 3 CTAs/SM: 4-byte keys {256x32, 384x20,
+// radix_sort onesweep tiles, all at 3 CTAs/SM: 4-byte keys {384x20, 256x32,
 // 256x24} (with 8-byte values each holds half the keys per thread); 8-byte
 // keys {256x16, 256x12, 384x10}.
 inline int radix_count(int) { return 3; }
 inline const char* radix_name(int key_bytes, int v) {
-  static const char* n4[] = { "256x32", "384x20", "256x24" };
+  static const char* n4[] = { "384x20", "256x32", "256x24" };
   static const char* n8[] = { "256x16", "256x12", "384x10" };
   return key_bytes == 4 ? n4[v] : n8[v];
 }

@@ -73,9 +73,7 @@ struct onesweep_args {
 //      16 bytes;
 //   B  the warps' match words while ranking (2 KB per warp), then the keys
 //      in local digit order, then the values in that order;
-//   W  each warp's digit offsets within the tile, then one digit byte per
-//      sorted position (the values' write-out needs the digits after the
-//      sorted keys have left B);
+//   W  each warp's digit offsets within the tile;
 //   plus the digits' global bases, scan scratch, the mbarrier and the tile id.
 template<typename K, typename V, int NT, int ITEMS>
 struct onesweep_layout {
@@ -87,9 +85,7 @@ struct onesweep_layout {
   static constexpr size_t a_off = 0;
   static constexpr size_t b_off = a_off + elem * tile + 16;
   static constexpr size_t w_off = b_off + elem * tile;
-  static constexpr size_t w_bytes =
-    ((size_t)num_warps * radix_bins * 4 > (size_t)tile ? (size_t)num_warps * radix_bins * 4
-                                                        : (size_t)tile + 15) & ~(size_t)15;
+  static constexpr size_t w_bytes = (size_t)num_warps * radix_bins * 4;
   static constexpr size_t gbase_off = w_off + w_bytes;
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
@@ -204,50 +200,58 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // Decoupled look-back of one digit: the sum of the counts of all predecessor
 // tiles.  `pred` is this digit's word in the nearest predecessor's row; there
-// are `num_pred` predecessors, 256 words apart.  Each round loads the status
-// of WINDOW predecessors at once (one L2 round trip) and consumes them in
-// order: aggregates are added, an inclusive prefix ends the walk, and an
-// unpublished status stops the round (the walk resumes there).  issue()
-// starts the first round early so its latency overlaps other work; finish()
-// completes the walk.  Bounded.
-template<int WINDOW>
+// are `num_pred` predecessors, 256 words apart.  issue() loads the status of
+// the nearest WINDOW predecessors (one L2 round trip) early, so its latency
+// overlaps other work; finish() consumes them in order (aggregates are added,
+// an inclusive prefix ends the walk, an unpublished status stops the round)
+// and continues, if needed, with rounds of WIDE predecessors each: the walk
+// usually reaches back a couple of dozen tiles, so wide later rounds save
+// round trips without holding WIDE registers across the overlapped work.
+// Bounded.
+template<int WINDOW, int WIDE = 4>
 struct lookback_window_t {
   uint32_t s[WINDOW];
   const uint32_t* pred;
   int left;
 
-  __device__ __forceinline__ void load() {
+  __device__ __forceinline__ void issue(const uint32_t* p, int num_pred) {
+    pred = p;
+    left = num_pred;
 #pragma unroll
     for(int k = 0; k < WINDOW; ++k)
       s[k] = k < left ? ld_relaxed(pred - k * radix_bins) : lb_inc;
   }
-  __device__ __forceinline__ void issue(const uint32_t* p, int num_pred) {
-    pred = p;
-    left = num_pred;
-    load();
+  // Consumes statuses in order; returns true when an inclusive prefix ended
+  // the walk, else advances `pred` / `left` past the aggregates used and
+  // sets `stalled` if an unpublished status stopped the round.
+  template<int N>
+  __device__ __forceinline__ bool consume(const uint32_t (&w)[N], uint32_t& excl, bool& stalled) {
+    int used = 0;
+    bool done = false;
+    stalled = false;
+#pragma unroll
+    for(int k = 0; k < N; ++k) {
+      if(!done && !stalled) {
+        const uint32_t flag = w[k] & ~lb_count;
+        if(!flag) {
+          stalled = true;
+        } else {
+          excl += w[k] & lb_count;
+          ++used;
+          done = flag == lb_inc;
+        }
+      }
+    }
+    pred -= used * radix_bins;
+    left -= used;
+    return done;
   }
   __device__ __forceinline__ uint32_t finish(int* error) {
     uint32_t excl = 0;
+    bool stalled;
+    if(consume(s, excl, stalled)) return excl;
     int spins = 0;
     while(true) {
-      int used = 0;
-      bool done = false, stalled = false;
-#pragma unroll
-      for(int k = 0; k < WINDOW; ++k) {
-        if(!done && !stalled) {
-          uint32_t flag = s[k] & ~lb_count;
-          if(!flag) {
-            stalled = true;
-          } else {
-            excl += s[k] & lb_count;
-            ++used;
-            done = flag == lb_inc;
-          }
-        }
-      }
-      if(done) return excl;
-      pred -= used * radix_bins;
-      left -= used;
       if(stalled) {
         ++spins;
         if(spins >= spin_limit ||
@@ -259,7 +263,11 @@ struct lookback_window_t {
         // other warps on this SM for a short while before polling again.
         __nanosleep(128);
       }
-      load();
+      uint32_t w[WIDE];
+#pragma unroll
+      for(int k = 0; k < WIDE; ++k)
+        w[k] = k < left ? ld_relaxed(pred - k * radix_bins) : lb_inc;
+      if(consume(w, excl, stalled)) return excl;
     }
   }
 };
@@ -279,7 +287,6 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   unsigned char* A = smem + L::a_off;
   unsigned char* B = smem + L::b_off;
   uint32_t* W = (uint32_t*)(smem + L::w_off);
-  uint8_t* Wb = (uint8_t*)(smem + L::w_off);
   int* gbase = (int*)(smem + L::gbase_off);
   uint32_t* stmp = (uint32_t*)(smem + L::scan_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
@@ -288,28 +295,33 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const int64_t base = t.base;
   const int valid = t.valid;
   const int tile = t.local;
-  // a.tma: both arrays start on 16 bytes.  A full tile is bulk-copied as
-  // the 16-byte-aligned window [kstart, kend) around it (the tile starts
-  // koff elements in); values likewise.  The window must lie inside the
-  // arrays (count elements), else the tile takes plain loads.  Without
-  // UNALIGNED the tile itself must start on 16 bytes (koff = voff = 0).
+  // a.tma: both arrays start on 16 bytes.  The tile's keys are bulk-copied
+  // as the 16-byte-aligned window [kstart, kend) around it (the tile starts
+  // koff elements in); values likewise.  A full tile whose whole window lies
+  // inside the array copies it all; otherwise (a ragged last tile) the window
+  // ends at the last whole 16 bytes before the tile's end, and threads load
+  // the positions after it with plain loads.  Without UNALIGNED a tile must
+  // start on 16 bytes to be copied.
   constexpr int64_t KV = 16 / sizeof(U);
   constexpr int64_t VV = HAS_V ? 16 / sizeof(V) : 1;
-  int64_t kstart = base, vstart = base, kend = base + TILE, vend = base + TILE;
-  bool bulk;
-  if constexpr(UNALIGNED) {
-    kstart = base & ~(KV - 1);
-    vstart = base & ~(VV - 1);
-    kend = (base + TILE + KV - 1) & ~(KV - 1);
-    vend = (base + TILE + VV - 1) & ~(VV - 1);
-    bulk = a.tma && valid == TILE && kend <= a.count && (!HAS_V || vend <= a.count);
-  } else {
-    bulk = a.tma && valid == TILE && 0 == (base & (KV - 1)) && 0 == (base & (VV - 1));
-  }
-  const int koff = UNALIGNED && bulk ? (int)(base - kstart) : 0;
-  const int voff = UNALIGNED && bulk ? (int)(base - vstart) : 0;
+  auto window = [&](int64_t per_vec, int64_t& start, int64_t& end) -> bool {
+    start = UNALIGNED ? (base & ~(per_vec - 1)) : base;
+    if(!UNALIGNED && (base & (per_vec - 1))) return false;
+    const int64_t full = (base + TILE + per_vec - 1) & ~(per_vec - 1);
+    end = valid == TILE && full <= a.count ? full : (base + valid) & ~(per_vec - 1);
+    return a.tma && end > base;
+  };
+  int64_t kstart = base, kend = base, vstart = base, vend = base;
+  const bool bulk_k = window(KV, kstart, kend);
+  const bool bulk_v = HAS_V && window(VV, vstart, vend);
+  const int koff = bulk_k ? (int)(base - kstart) : 0;
+  const int voff = bulk_v ? (int)(base - vstart) : 0;
+  // Tile positions from kfill (vfill) on are loaded by the threads.
+  const int kfill = bulk_k ? (int)min((int64_t)TILE, kend - base) : 0;
+  const int vfill = bulk_v ? (int)min((int64_t)TILE, vend - base) : 0;
+  const uint32_t vparity = bulk_k ? 1 : 0;       // mbarrier phase of the values' copy
 
-  if(bulk && tid == 0) {
+  if(bulk_k && tid == 0) {
     const uint32_t kbytes = (uint32_t)(sizeof(U) * (kend - kstart));
     mbar_arrive_expect_tx(bar, kbytes);
     bulk_load(A, a.keys_in + kstart, kbytes, bar);
@@ -337,20 +349,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   const int warp_base = warp * 32 * ITEMS;
   const int rem = valid - warp_base - lane;
   U* const ak = (U*)A + koff + warp_base + lane;        // this thread's staged keys
-  if(bulk) {
-    // Only warp 0 polls the barrier; the other warps sleep at the CTA
-    // barrier below instead of spending issue slots.  The mbarrier phase
-    // completion makes the copied bytes visible to warp 0, and the CTA
-    // barrier passes that on to every thread.
-    bool ok = true;
-    if(warp == 0) ok = mbar_wait_bounded(bar, 0, a.error);
-    if(__syncthreads_or(!ok)) {
-      // The copy did not complete in time: wait once more (bounded) so no
-      // bulk copy is still writing this CTA's shared memory, then leave.
-      if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
-      return;
-    }
-  } else {
+  if(kfill < TILE) {
     // Plain loads; positions past the tile's end take the largest radix
     // bits, so they rank last (after every real key with digit 255).
     U fill = ~(U)0;
@@ -360,8 +359,22 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     }
     const U* src = a.keys_in + base + warp_base + lane;
 #pragma unroll 4
-    for(int i = 0; i < ITEMS; ++i) ak[32 * i] = 32 * i < rem ? src[32 * i] : fill;
-    __syncthreads();
+    for(int i = 0; i < ITEMS; ++i)
+      if(warp_base + 32 * i + lane >= kfill) ak[32 * i] = 32 * i < rem ? src[32 * i] : fill;
+  }
+  {
+    // Only warp 0 polls the barrier; the other warps sleep at the CTA
+    // barrier below instead of spending issue slots.  The mbarrier phase
+    // completion makes the copied bytes visible to warp 0, and the CTA
+    // barrier passes that on to every thread.
+    bool ok = true;
+    if(bulk_k && warp == 0) ok = mbar_wait_bounded(bar, 0, a.error);
+    if(__syncthreads_or(!ok)) {
+      // The copy did not complete in time: wait once more (bounded) so no
+      // bulk copy is still writing this CTA's shared memory, then leave.
+      if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
+      return;
+    }
   }
   bool check_uniform;
   {
@@ -472,7 +485,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   __syncthreads();
   // A is free: the values' bulk copy overlaps the look-back and the key
   // write-out.
-  if(HAS_V && bulk && tid == 0) {
+  if(bulk_v && tid == 0) {
     const uint32_t vbytes = (uint32_t)(sizeof(V) * (vend - vstart));
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(bar, vbytes);
@@ -492,9 +505,11 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   __syncthreads();
 
   // Write out in local order: consecutive threads hit consecutive addresses
-  // inside each digit's run.  CHUNK loads, then CHUNK stores.  Each
-  // position's digit is kept (W is free now) for the values.
+  // inside each digit's run.  CHUNK loads, then CHUNK stores.  The values
+  // are written out by the same threads at the same positions, so each
+  // thread keeps its positions' digits, packed four per register.
   U* keys_out = a.keys_out + t.out_base;
+  uint32_t dq[(ITEMS + 3) / 4];
 #pragma unroll
   for(int j0 = 0; j0 < ITEMS; j0 += CHUNK) {
     U u[CHUNK];
@@ -505,7 +520,8 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       if(j0 + c < ITEMS && idx < valid) {
         u[c] = ((const U*)B)[idx];
         const uint32_t d = extract_digit(u[c], a.shift, 8);
-        if(HAS_V) Wb[idx] = (uint8_t)d;
+        const int j = j0 + c;
+        if(HAS_V) dq[j >> 2] = (j & 3) ? dq[j >> 2] | (d << (8 * (j & 3))) : d;
         dst[c] = (uint32_t)gbase[d] + idx;
       }
     }
@@ -527,18 +543,18 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
   if constexpr(HAS_V) {
     V* const av = (V*)A + voff + warp_base + lane;     // this thread's staged values
-    if(bulk) {
-      bool ok = true;
-      if(warp == 0) ok = mbar_wait_bounded(bar, 1, a.error);
-      if(__syncthreads_or(!ok)) {
-        if(warp == 0) mbar_wait_bounded(bar, 1, a.error);
-        return;
-      }
-    } else {
-      __syncthreads();                     // the sorted keys have left B
+    // The sorted keys must have left B, and (when copied) the values arrived.
+    bool ok = true;
+    if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error);
+    if(__syncthreads_or(!ok)) {
+      if(warp == 0) mbar_wait_bounded(bar, vparity, a.error);
+      return;
+    }
+    if(vfill < valid) {
       const V* src = a.vals_in + base + warp_base + lane;
 #pragma unroll 4
-      for(int i = 0; i < ITEMS; ++i) if(32 * i < rem) av[32 * i] = src[32 * i];
+      for(int i = 0; i < ITEMS; ++i)
+        if(32 * i < rem && warp_base + 32 * i + lane >= vfill) av[32 * i] = src[32 * i];
       __syncwarp();                        // each warp reads only its own rows
     }
 #pragma unroll
@@ -554,8 +570,9 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       for(int c = 0; c < CHUNK; ++c) {
         const int idx = (j0 + c) * NT + tid;
         if(j0 + c < ITEMS && idx < valid) {
+          const int j = j0 + c;
           v[c] = ((const V*)B)[idx];
-          dst[c] = (uint32_t)gbase[Wb[idx]] + idx;
+          dst[c] = (uint32_t)gbase[(dq[j >> 2] >> (8 * (j & 3))) & 0xffu] + idx;
         }
       }
 #pragma unroll
