@@ -508,7 +508,7 @@ def wl_segsort(args, mg, torch):
     sorted by per-segment plain radix_sort calls on the same GPU, both as a
     host loop and captured into one CUDA graph."""
     rng = np.random.default_rng(SEED + 8)
-    off = _lognormal_offsets(rng, 100_000)
+    off = _lognormal_offsets(rng, args.seg_count)
     n = int(off[-1])
     keys = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
     vals = np.arange(n, dtype=np.uint32)
@@ -535,6 +535,13 @@ def wl_segsort(args, mg, torch):
     roof, kernels = _roofline(ctx, run, restore, 3,
                               {"seg_small_sort": 16 * small_keys,
                                "seg_onesweep_pass": 16 * (n - small_keys)})
+    if args.no_plain:
+        cfg = {"workload": "segmented_sort u32 keys + u32 values, %d lognormal(ln 256, 2) "
+                           "segments clipped to [1, 2^20], %d keys" % (len(off) - 1, n),
+               "count": n, "segments": len(off) - 1, "alg_bytes_per_key": 16,
+               "l2": "inputs larger than L2, restored by a device copy outside the step's events"}
+        return _line("Mkeys/s", "Mkeys/s", n, 16 * n, ms, steps, warmup, launches, clk, roof,
+                     kernels, cfg, "u32", checks)
     # Per-segment plain calls (the C ABI's radix sort on each segment).
     lib = mg.lib()
     pctx = mg.Context(0, use_torch_stream=False)
@@ -580,9 +587,9 @@ def wl_segsort(args, mg, torch):
     graph_ok = bool(np.array_equal(wk.numpy(), gk))
     g.close()
     mean = sum(ms) / len(ms)
-    cfg = {"workload": "segmented_sort u32 keys + u32 values, 100000 lognormal(ln 256, 2) "
-                       "segments clipped to [1, 2^20], %d keys" % n,
-           "count": n, "segments": 100_000, "alg_bytes_per_key": 16,
+    cfg = {"workload": "segmented_sort u32 keys + u32 values, %d lognormal(ln 256, 2) "
+                       "segments clipped to [1, 2^20], %d keys" % (len(off) - 1, n),
+           "count": n, "segments": len(off) - 1, "alg_bytes_per_key": 16,
            "l2": "inputs larger than L2, restored by a device copy outside the step's events"}
     extra = {"plain_calls": {
         "host_loop_ms": loop_ms, "graph_ms": statistics.median(graph_ms),
@@ -597,7 +604,7 @@ def wl_segscan(args, mg, torch):
     """The segmented-sort segments over int32 U[0,100) values, inclusive
     plus; 8 B/element."""
     rng = np.random.default_rng(SEED + 8)
-    off = _lognormal_offsets(rng, 100_000)
+    off = _lognormal_offsets(rng, args.seg_count)
     n = int(off[-1])
     x = rng.integers(0, 100, n).astype(np.int32)
     ctx = mg.Context(0)
@@ -614,9 +621,9 @@ def wl_segscan(args, mg, torch):
     start = np.repeat(np.concatenate([[0], c])[off[:-1]], np.diff(off))
     ok = bool(np.array_equal(y, (c - start).astype(np.int32)))
     roof, kernels = _roofline(ctx, run, lambda i: None, 3, {"seg_scan": 8 * n})
-    cfg = {"workload": "segmented_scan int32 U[0,100), inclusive plus, the 100000 "
-                       "lognormal segments, %d elements" % n,
-           "count": n, "segments": 100_000, "alg_bytes_per_elem": 8,
+    cfg = {"workload": "segmented_scan int32 U[0,100), inclusive plus, %d "
+                       "lognormal segments, %d elements" % (len(off) - 1, n),
+           "count": n, "segments": len(off) - 1, "alg_bytes_per_elem": 8,
            "l2": "inputs larger than L2"}
     return _line("Melems/s", "Melems/s", n, 8 * n, ms, steps, warmup, launches, clk, roof,
                  kernels, cfg, "int32", {"matches_host_segmented_scan": ok})
@@ -795,6 +802,111 @@ def wl_serving(args, mg, torch):
             "p50_ms": hi["server"]["p50_ms"], "p99_ms": hi["server"]["p99_ms"]}
 
 
+def wl_radix_small(args, mg, torch):
+    """Many small sorts: 64 plain radix sorts of 4096 u32 keys + u32 values per
+    step, each one CTA (radix_sort_cta); 16 B/key."""
+    n = args.n if args.n != N_KEYS else 4096
+    batch = 64
+    rng = np.random.default_rng(SEED + 10)
+    keys = rng.integers(0, 2 ** 32, n * batch, dtype=np.uint64).astype(np.uint32)
+    vals = np.tile(np.arange(n, dtype=np.uint32), batch)
+    ctx = mg.Context(0)
+    pk, pv = mg.DeviceArray.from_numpy(keys), mg.DeviceArray.from_numpy(vals)
+    wk, wv = mg.DeviceArray(n * batch, np.uint32), mg.DeviceArray(n * batch, np.uint32)
+    lib = mg.lib()
+
+    def restore(i):
+        wk.copy_from(pk)
+        wv.copy_from(pv)
+
+    def run(i):
+        for b in range(batch):
+            ctx._check(lib.mgpu_radix_sort(ctx.handle, 1, wk.ptr + 4 * n * b, 4,
+                                           wv.ptr + 4 * n * b, n, None, None))
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
+    gk, gv = wk.numpy().reshape(batch, n), wv.numpy().reshape(batch, n)
+    ok = all(stable_sort_checks(keys[b * n:(b + 1) * n], gk[b], gv[b])["keys_ascend"] and
+             np.array_equal(keys[b * n:(b + 1) * n][gv[b]], gk[b]) for b in range(batch))
+    roof, kernels = _roofline(ctx, run, restore, 3, {"radix_sort_cta": 16 * n})
+    cfg = {"workload": "radix_sort_kv u32 keys + u32 values, %d sorts of %d keys per step" % (
+        batch, n), "count": n * batch, "alg_bytes_per_key": 16,
+        "l2": "inputs restored by a device copy outside the step's events"}
+    return _line("Mkeys/s", "Mkeys/s", n * batch, 16 * n * batch, ms, steps, warmup, launches,
+                 clk, roof, kernels, cfg, "u32", {"sorted_and_permuted": ok})
+
+
+def wl_reduce(args, mg, torch):
+    """2^28 int32 U[0,100) plus-reduce; 4 B/element."""
+    n = args.n if args.n != N_KEYS else 1 << 28
+    rng = np.random.default_rng(SEED + 11)
+    x = rng.integers(0, 100, n).astype(np.int32)
+    ctx = mg.Context(0)
+    dx, dout = mg.DeviceArray.from_numpy(x), mg.DeviceArray(1, np.int32)
+
+    def run(i):
+        ctx.reduce(dx, dout)
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, lambda i: None, steps, warmup, 0)
+    s64 = int(np.sum(x, dtype=np.int64))
+    ok = int(dout.numpy()[0]) == ((s64 + 2 ** 31) % 2 ** 32) - 2 ** 31     # int32 wrap
+    roof, kernels = _roofline(ctx, run, lambda i: None, 3, {"reduce": 4 * n})
+    cfg = {"workload": "reduce int32 U[0,100), %d elements, plus" % n, "count": n,
+           "alg_bytes_per_elem": 4, "l2": "inputs larger than L2"}
+    return _line("Melems/s", "Melems/s", n, 4 * n, ms, steps, warmup, launches, clk, roof,
+                 kernels, cfg, "int32", {"matches_host_sum": ok})
+
+
+def wl_scan_noalloc(args, mg, torch):
+    """2^28 int32 U[0,100) exclusive plus-scan through mgpu_scan_noalloc
+    (one tile per CTA, scratch inside the library); 8 B/element."""
+    import ctypes
+    n = args.n if args.n != N_KEYS else 1 << 28
+    rng = np.random.default_rng(SEED + 3)
+    x = rng.integers(0, 100, n).astype(np.int32)
+    dx, dy = mg.DeviceArray.from_numpy(x), mg.DeviceArray(n, np.int32)
+    lib = mg.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+
+    def run():
+        rc = lib.mgpu_scan_noalloc(ctypes.c_void_p(stream), 0, 0, 0, ctypes.c_void_p(dx.ptr),
+                                   ctypes.c_void_p(dy.ptr), n, None, None)
+        if rc:
+            raise RuntimeError("mgpu_scan_noalloc: status %d" % rc)
+
+    for _ in range(max(3, args.warmup)):
+        run()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    for i in range(args.steps):
+        ev[i][0].record()
+        run()
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    status = lib.mgpu_scan_noalloc_status(ctypes.c_void_p(stream))
+    ref = np.cumsum(x, dtype=np.int64).astype(np.int32)
+    ok = bool(np.array_equal(dy.numpy(), np.concatenate([[0], ref[:-1]]).astype(np.int32)))
+    mean = sum(ms) / len(ms)
+    peak, src = _peak()
+    achieved = 8 * n / (mean * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "scan_kernel (one tile per CTA)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": src, "launch_ms": mean, "bytes_per_launch": 8 * n}
+    cfg = {"workload": "scan_noalloc int32 U[0,100), %d elements, exclusive plus" % n,
+           "count": n, "alg_bytes_per_elem": 8, "l2": "inputs larger than L2"}
+    return _line("Melems/s", "Melems/s", n, 8 * n, ms, args.steps, max(3, args.warmup),
+                 2 * args.steps, clk, roof, {}, cfg, "int32",
+                 {"matches_host_scan": ok, "device_status_ok": status == 0})
+
+
 WORKLOADS = {
     "radix_u64": lambda a, m, t: wl_radix_wide(a, m, t, "u64"),
     "radix_f32": lambda a, m, t: wl_radix_wide(a, m, t, "f32bits"),
@@ -806,6 +918,9 @@ WORKLOADS = {
     "segsort": wl_segsort,
     "segscan": wl_segscan,
     "serving": wl_serving,
+    "radix_small": wl_radix_small,
+    "reduce": wl_reduce,
+    "scan_noalloc": wl_scan_noalloc,
 }
 
 
@@ -877,6 +992,10 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the short runs of the other configurations")
     ap.add_argument("--secondary-steps", type=int, default=10)
+    ap.add_argument("--seg-count", type=int, default=100_000,
+                    help="segsort/segscan: number of lognormal segments")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="segsort: skip the per-segment plain-call comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
