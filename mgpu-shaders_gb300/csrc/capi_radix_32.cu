@@ -14,6 +14,16 @@ mgpu_status_t sort_shape(mgpu_context* c, K* keys, V* vals, int64_t count, void*
   return radix_sort_kv<NT, VT, MINB, DEV>(aux, aux_size, c->ctx, keys, vals, count, d_count);
 }
 
+// A 4-bit-digit shape (eight passes over 4-byte keys), CTAs per SM as the
+// C++ knobs derive them.
+template<int NT, int VT4, typename K, typename V>
+mgpu_status_t sort_shape4(mgpu_context* c, K* keys, V* vals, int64_t count, void* aux,
+  size_t* aux_size) {
+  constexpr int VT = radix_elem_bytes<K, V>() == 8 ? VT4 / 2 : VT4;
+  typedef radix_knobs<K, V, NT, VT, 4> R;
+  return radix_sort_kv<R::NT, R::VT, R::MINB, false, 4>(aux, aux_size, c->ctx, keys, vals, count);
+}
+
 mgpu_status_t radix_sort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys, int val_bytes,
   void* vals, int64_t count, int variant, void* aux, size_t* aux_size, const int64_t* d_count) {
   auto go_key = [&](auto* kp) -> mgpu_status_t {
@@ -27,6 +37,8 @@ mgpu_status_t radix_sort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
       switch(variant) {
         case 1: return sort_shape<256, 32, 3>(c, k, v, count, aux, aux_size, nullptr);
         case 2: return sort_shape<256, 24, 3>(c, k, v, count, aux, aux_size, nullptr);
+        case 3: return sort_shape4<256, 16>(c, k, v, count, aux, aux_size);
+        case 4: return sort_shape4<128, 16>(c, k, v, count, aux, aux_size);
         default: return sort_shape<384, 20, 3>(c, k, v, count, aux, aux_size, nullptr);
       }
     };

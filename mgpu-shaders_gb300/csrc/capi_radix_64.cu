@@ -17,6 +17,16 @@ mgpu_status_t radix_sort_w64(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
       switch(variant) {
         case 1: return radix_sort_kv<256, 12, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
         case 2: return radix_sort_kv<384, 10, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
+        case 3: {
+          typedef radix_knobs<K, V, 256, 16, 4> R;
+          return radix_sort_kv<R::NT, R::VT, R::MINB, false, 4>(aux, aux_size, c->ctx, (K*)keys,
+            (V*)vals, count);
+        }
+        case 4: {
+          typedef radix_knobs<K, V, 128, 16, 4> R;
+          return radix_sort_kv<R::NT, R::VT, R::MINB, false, 4>(aux, aux_size, c->ctx, (K*)keys,
+            (V*)vals, count);
+        }
         default: return radix_sort_kv<256, 16, 3>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count);
       }
     };

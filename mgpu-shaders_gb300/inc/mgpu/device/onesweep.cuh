@@ -123,14 +123,15 @@ __device__ __forceinline__ void scan_256_pair(uint32_t& x, uint32_t& y, uint32_t
 // and lane l updates copy l % LANES, so the 32 lanes of a warp hit 32 (or,
 // with 16 copies, at worst 2 x 16) different banks and the shared-memory
 // atomics do not conflict; the copies are summed before one global atomic
-// per bin and CTA.  Dynamic shared memory: PASSES * 256 * LANES counters.
-template<typename K, int NT, int PASSES, int LANES>
+// per bin and CTA.  Dynamic shared memory: PASSES * 2^BITS * LANES counters
+// (BITS: digit width, 8 or 4).
+template<typename K, int NT, int PASSES, int LANES, int BITS = 8>
 __global__ void __launch_bounds__(NT)
 radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised,
   const int64_t* count_ptr) {
   typedef typename radix_key<K>::bits_t U;
   if(count_ptr) count = max((int64_t)0, min(*count_ptr, count));
-  constexpr int BINS = PASSES * radix_bins;
+  constexpr int BINS = PASSES << BITS;
   extern __shared__ __align__(16) uint32_t sh[];
   const int tid = threadIdx.x;
   for(int i = tid; i < BINS * LANES / 4; i += NT)
@@ -144,7 +145,7 @@ radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised,
     U u = radix_key<K>::to_bits(key);
 #pragma unroll
     for(int p = 0; p < PASSES; ++p)
-      atomicAdd(&sh[(p * radix_bins + extract_digit(u, 8 * p, 8)) * LANES + copy], 1u);
+      atomicAdd(&sh[((p << BITS) + extract_digit(u, BITS * p, BITS)) * LANES + copy], 1u);
   };
   constexpr int per_vec = 16 / sizeof(K);
   int64_t num_vec = vectorised ? count / per_vec : 0;
@@ -200,15 +201,16 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // Decoupled look-back of one digit: the sum of the counts of all predecessor
 // tiles.  `pred` is this digit's word in the nearest predecessor's row; there
-// are `num_pred` predecessors, 256 words apart.  issue() loads the status of
+// are `num_pred` predecessors, ROW words apart.  issue() loads the status of
 // the nearest WINDOW predecessors (one L2 round trip) early, so its latency
 // overlaps other work; finish() consumes them in order (aggregates are added,
 // an inclusive prefix ends the walk, an unpublished status stops the round)
-// and continues, if needed, with rounds of WIDE predecessors each: the walk
-// usually reaches back a couple of dozen tiles, so wide later rounds save
-// round trips without holding WIDE registers across the overlapped work.
-// Bounded.
-template<int WINDOW, int WIDE = 4>
+// and continues, if needed, with rounds of WIDE predecessors each.  On a
+// 2^28-key sort the walk reaches back about 20 tiles in 5-6 rounds; rounds of
+// 16 or 32 predecessors took fewer rounds but longer ones, and the walks grew,
+// so WIDE stays 4.  Bounded.  ROW: status words per tile (one per digit: 256
+// for 8-bit digits, 16 for 4-bit ones).
+template<int WINDOW, int WIDE = 4, int ROW = radix_bins>
 struct lookback_window_t {
   uint32_t s[WINDOW];
   const uint32_t* pred;
@@ -219,7 +221,7 @@ struct lookback_window_t {
     left = num_pred;
 #pragma unroll
     for(int k = 0; k < WINDOW; ++k)
-      s[k] = k < left ? ld_relaxed(pred - k * radix_bins) : lb_inc;
+      s[k] = k < left ? ld_relaxed(pred - k * ROW) : lb_inc;
   }
   // Consumes statuses in order; returns true when an inclusive prefix ended
   // the walk, else advances `pred` / `left` past the aggregates used and
@@ -242,7 +244,7 @@ struct lookback_window_t {
         }
       }
     }
-    pred -= used * radix_bins;
+    pred -= used * ROW;
     left -= used;
     return done;
   }
@@ -266,7 +268,7 @@ struct lookback_window_t {
       uint32_t w[WIDE];
 #pragma unroll
       for(int k = 0; k < WIDE; ++k)
-        w[k] = k < left ? ld_relaxed(pred - k * radix_bins) : lb_inc;
+        w[k] = k < left ? ld_relaxed(pred - k * ROW) : lb_inc;
       if(consume(w, excl, stalled)) return excl;
     }
   }

@@ -108,15 +108,35 @@ status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t
   return scan<scan_type, nt, vt, persistent>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
 }
 
+// The launch shape the reference's scan<nt, vt> knobs select: nt threads
+// (rounded up to whole warps, at least two), vt elements per thread rounded up
+// to whole 16-byte vectors, on the persistent deferred look-back kernel; CTAs
+// per SM from its shared memory (one nt x vt stage) and a 64-register budget.
+template<typename T, int nt, int vt>
+struct scan_knobs {
+  static constexpr int per = 16 / (int)sizeof(T);
+  static constexpr int nt_w = (nt + 31) / 32 * 32;
+  static constexpr int NT = nt_w < 64 ? 64 : (nt_w > 1024 ? 1024 : nt_w);
+  static constexpr int vt_v = (vt + per - 1) / per * per;
+  static constexpr int VT = vt_v < per ? per : vt_v;
+  static constexpr int by_smem = (int)(233472 / ((size_t)sizeof(T) * NT * VT + 16 + 1024));
+  static constexpr int by_regs = 65536 / (NT * 64);
+  static constexpr int m = by_smem < by_regs ? by_smem : by_regs;
+  static constexpr int MINB = m < 1 ? 1 : (m > 8 ? 8 : m);
+};
+
 // The reference's exact template shape, scan<nt, vt>(aux_data, aux_size,
-// cmd, data, count, init, op) (vk/scan.hxx:10-13): there nt and vt only choose
-// the launch shape, so the in-place exclusive scan runs with the shape tuned
-// for the element width.  (nt and vt have no defaults here, so a call without
+// cmd, data, count, init, op) (vk/scan.hxx:10-13): the in-place exclusive
+// scan with the launch shape scan_knobs derives from nt and vt (the reference
+// default <128, 7> runs 128 x 8).  The result does not depend on the shape
+// beyond float rounding.  (nt and vt have no defaults here, so a call without
 // template arguments selects the form above.)
 template<int nt, int vt, typename T, typename op_t = plus_t<T>>
 status_t scan(void* aux_data, size_t& aux_size, context_t& ctx, T* data, int64_t count,
   T init = op_t::identity(), op_t op = op_t()) {
-  return scan<scan_type_exc>(aux_data, &aux_size, ctx, (const T*)data, count, data, init, op);
+  typedef scan_knobs<T, nt, vt> S;
+  return scan<scan_type_exc, S::NT, S::VT, 1, S::MINB>(aux_data, &aux_size, ctx, (const T*)data,
+    count, data, init, op);
 }
 
 // Memcache form.

@@ -118,10 +118,15 @@ int main() {
     bool ok = true;
     for(int i = 0; i < count; ++i) ok &= h[i] == (int)((int64_t)i * (i - 1) / 2);
     CHECK(ok, "scan_exclusive_in_place");
-    // The same call with the reference's explicit launch knobs and operator.
+    // The same call with the reference's explicit launch knobs and operator:
+    // a different launch shape, so it is sized with its own first call.
     for(int i = 0; i < count; ++i) h[i] = i;
     context.memcpy(gpu, h.data(), sizeof(int) * count);
-    scan<128, 7>(aux_data, aux_size, context, gpu, count, 0, plus_t<int>());
+    void* aux_knobs = nullptr;
+    size_t aux_knobs_size = 0;
+    scan<128, 7>(aux_knobs, aux_knobs_size, context, gpu, count, 0, plus_t<int>());
+    aux_knobs = context.alloc_gpu(aux_knobs_size);
+    if(scan<128, 7>(aux_knobs, aux_knobs_size, context, gpu, count, 0, plus_t<int>())) return 3;
     context.memcpy(h.data(), gpu, sizeof(int) * count);
     if(context.synchronize()) return 2;
     ok = true;
@@ -147,6 +152,30 @@ int main() {
     context.memcpy(h.data(), gpu, sizeof(uint32_t) * count);
     if(context.synchronize()) return 2;
     CHECK(h == ref, "radix_sort_keys");
+  }
+
+  // The reference's default radix_sort template, <128, 15, 4>: 4-bit digits
+  // (eight passes), 128 threads, 16 keys per thread; the same permutation.
+  {
+    const int count = 1000003;
+    std::vector<uint32_t> h(count), ref;
+    for(auto& v : h) v = (uint32_t)rand() * 2654435761u;
+    ref = h;
+    std::sort(ref.begin(), ref.end());
+    uint32_t* gpu = context.alloc_gpu<uint32_t>(count);
+    context.memcpy(gpu, h.data(), sizeof(uint32_t) * count);
+    void* aux_data = nullptr;
+    size_t aux_size = 0;
+    radix_sort<128, 15, 4>(aux_data, aux_size, context, gpu, count);
+    aux_data = context.alloc_gpu(aux_size);
+    const int64_t launches0 = context.launches;
+    if(radix_sort<128, 15, 4>(aux_data, aux_size, context, gpu, count)) return 3;
+    const int64_t launches = context.launches - launches0;
+    context.memcpy(h.data(), gpu, sizeof(uint32_t) * count);
+    if(context.synchronize()) return 2;
+    CHECK(h == ref, "radix_sort_keys_4bit");
+    // Histogram + eight 4-bit passes, where the 8-bit shape runs four.
+    CHECK(launches == 9, "radix_sort_4bit_passes");
   }
   return 0;
 }

@@ -30,7 +30,8 @@ def test_cpp_template_api(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     for name in ["launch_transform", "mergesort_user_comparator", "merge_keys",
-                 "scan_exclusive_in_place", "radix_sort_keys"]:
+                 "scan_exclusive_in_place", "radix_sort_keys", "radix_sort_keys_4bit",
+                 "radix_sort_4bit_passes"]:
         assert "ok " + name in r.stdout
 
 

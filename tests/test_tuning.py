@@ -77,3 +77,47 @@ def test_autotune_records_and_round_trips(mgpu, tmp_path):
     assert c.tuning_get("scan", np.float32, 0, 1 << 20) == b2
     c.close()
     c2.close()
+
+
+@pytest.mark.parametrize("kt", [np.uint32, np.int32, np.float32, np.uint64, np.float64])
+@pytest.mark.parametrize("vb", [0, 4, 8])
+def test_4bit_digit_variants_are_exact(mgpu, ctx, oracle, rng, kt, vb):
+    """The 4-bit-digit passes (the reference's default digit width) give the
+    same permutation as the oracle, for every key type and value width, on
+    a ragged size and on one below a tile."""
+    names = ctx.tuning_variants("radix", kt)
+    four = [i for i, nm in enumerate(names) if nm.endswith("/4b")]
+    assert four and len(four) < len(names)          # both digit widths are variants
+    vdt = {0: None, 4: np.uint32, 8: np.uint64}[vb]
+    try:
+        for n in (300_017, 9_001):
+            k = gen_keys(rng, n, kt)
+            v = None if vdt is None else np.arange(n, dtype=vdt)
+            ok, ov = oracle.radix_sort(k, v)
+            for var in four:
+                ctx.tuning_set("radix", kt, vb, -1, var)
+                dk = mgpu.DeviceArray.from_numpy(k)
+                dv = None if v is None else mgpu.DeviceArray.from_numpy(v)
+                ctx.radix_sort(dk, dv)
+                ctx.synchronize()
+                assert np.array_equal(dk.numpy().view(np.uint8), ok.view(np.uint8)), names[var]
+                if v is not None:
+                    assert np.array_equal(dv.numpy(), ov), names[var]
+    finally:
+        ctx.tuning_set("radix", kt, vb, -1, 0)
+
+
+def test_autotune_chooses_the_digit_width(mgpu):
+    """The autotuner times both digit widths and records the fastest variant
+    per size bucket; each chosen variant's name states its digit width."""
+    c = mgpu.Context(0)
+    names = c.tuning_variants("radix", np.uint32)
+    widths = {4 if nm.endswith("/4b") else 8 for nm in names}
+    assert widths == {4, 8}
+    chosen = {}
+    for n in (1 << 16, 1 << 20, 1 << 24):
+        best, ms = c.autotune("radix", np.uint32, 4, n, reps=2)
+        assert ms > 0 and c.tuning_get("radix", np.uint32, 4, n) == best
+        chosen[n] = (names[best], 4 if names[best].endswith("/4b") else 8)
+    print("autotuned radix variants (size: name, digit bits):", chosen)
+    c.close()
