@@ -694,7 +694,8 @@ def wl_serving(args, mg, torch):
     sat_rps = len(order) / sat_s
     sat_line = {"requests": len(order), "seconds": sat_s, "requests_per_s": sat_rps,
                 "mkeys_per_s": elems[order].sum() / sat_s / 1e6, "p50_ms": sat["p50_ms"],
-                "p99_ms": sat["p99_ms"], "peak_bytes": sat["peak_bytes"]}
+                "p99_ms": sat["p99_ms"], "peak_bytes": sat["peak_bytes"],
+                "coalesced_requests": sat["coalesced"], "coalesced_batches": sat["batches"]}
 
     # Serial plain calls: one context, device buffers sized for the largest request.
     ctx = mg.Context(0, use_torch_stream=False)
@@ -781,7 +782,8 @@ def wl_serving(args, mg, torch):
             "server": {"requests_per_s": num / span, "mkeys_per_s": elems[picks].sum() / span / 1e6,
                        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
                        "max_ms": st["max_ms"], "failed": st["failed"],
-                       "peak_bytes": st["peak_bytes"]},
+                       "peak_bytes": st["peak_bytes"], "coalesced_requests": st["coalesced"],
+                       "coalesced_batches": st["batches"]},
             "serial_plain_calls": {"requests_per_s": num / serial_span,
                                    "mkeys_per_s": elems[picks].sum() / serial_span / 1e6,
                                    "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99)}})

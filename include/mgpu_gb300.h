@@ -277,8 +277,13 @@ MGPU_API mgpu_status_t mgpu_cache_reserve(mgpu_context_t* ctx, size_t bytes);
  * admitted requests copy their host inputs into device buffers drawn from a
  * stream-ordered pool that stays resident, run the primitive on the slot's
  * stream, copy the results back and release their memory, so requests that
- * arrive while others run overlap with them.  Host buffers must stay valid
- * until the request completes (pinned memory gives asynchronous copies). */
+ * arrive while others run overlap with them.  Small sorts and integer scans
+ * (at most 2^16 elements) queued together with others of the same kind (op,
+ * key type, value width, scan type and operator) are coalesced: up to 512 of
+ * them (2^22 elements) run as one segmented sort or scan over a packed
+ * buffer, one launch sequence for the batch; each result is byte-identical to
+ * the one the request gets alone.  Host buffers must stay valid until the
+ * request completes (pinned memory gives asynchronous copies). */
 typedef enum mgpu_request_op_t {
   MGPU_REQ_SORT = 0,   /* radix sort of keys (+ values), in place on device */
   MGPU_REQ_MERGE = 1,  /* merge of sorted A and B (+ values) */
@@ -306,6 +311,8 @@ typedef struct mgpu_server_stats_t {
   int64_t elements;        /* sum of request element counts completed */
   double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> completion */
   size_t peak_bytes;       /* largest admitted footprint total */
+  int64_t coalesced;       /* requests that ran in coalesced batches */
+  int64_t batches;         /* coalesced batches launched */
 } mgpu_server_stats_t;
 
 typedef struct mgpu_server mgpu_server_t;
@@ -352,6 +359,21 @@ MGPU_API int64_t mgpu_launch_count(mgpu_context_t* ctx);
  * and the kernel returns, so the next mgpu_synchronize reports that status and
  * the context stays usable.  limit: 1 .. 2^22. */
 MGPU_API mgpu_status_t mgpu_selftest_bounded_wait(mgpu_context_t* ctx, int limit);
+/* Polls (1 .. 2^22) after which the look-back and bulk-copy waits of the
+ * radix-sort passes launched from this context give up and raise
+ * MGPU_ERR_LOOKBACK_TIMEOUT; 0 restores the library's limit (2^22 polls,
+ * seconds of wall time).  A smaller limit detects a stalled predecessor
+ * sooner; a limit too small for the load can raise false timeouts. */
+MGPU_API mgpu_status_t mgpu_set_wait_limit(mgpu_context_t* ctx, int polls);
+/* Runs the production radix-sort pass kernel (u32 keys + u32 values, the
+ * default tile shape) over two tiles with its tile counter advanced past
+ * tile 0, so the one CTA launched takes tile 1 and its decoupled look-back
+ * waits on a predecessor that never publishes.  With the context's wait
+ * limit (mgpu_set_wait_limit) the wait runs out, the pass records
+ * MGPU_ERR_LOOKBACK_TIMEOUT and returns; the next mgpu_synchronize reports
+ * it.  Every store stays inside the call's own buffers.  Synchronises and
+ * allocates its own buffers. */
+MGPU_API mgpu_status_t mgpu_selftest_lookback_timeout(mgpu_context_t* ctx);
 
 #ifdef __cplusplus
 }

@@ -54,3 +54,57 @@ mgpu_status_t radix_sort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
   }
   return MGPU_ERR_INVALID_ARG;
 }
+
+// Failure-path self test of the production look-back (mgpu_gb300.h): the
+// default u32 key-value pass kernel over two tiles of zero keys, tile counter
+// advanced to 1, one CTA.  That CTA claims tile 1 and waits on tile 0's
+// look-back row, which stays zero; the wait gives up after the context's
+// limit.  Tile 1 then stores at offsets 0 .. tile-1 (the look-back prefix it
+// could not read counts as 0), inside the two-tile output buffers.
+extern "C" mgpu_status_t mgpu_selftest_lookback_timeout(mgpu_context_t* c) {
+  MGPU_CHECK_CTX(c);
+  using namespace mgpu::device;
+  typedef radix_tuning<4> T;
+  constexpr int nt = T::nt, vt = T::vt, minb = T::min_blocks;
+  typedef onesweep_layout<uint32_t, uint32_t, nt, vt> L;
+  constexpr int64_t n = 2 * (int64_t)nt * vt;
+  auto kernel = onesweep_pass<uint32_t, uint32_t, nt, vt, minb, 4, false>;
+  context_t& ctx = c->ctx;
+  if(!ctx.allow_smem(kernel, L::bytes)) return MGPU_ERR_CUDA;
+  // keys in/out, values in/out, 256 digit counts, two look-back rows, counter
+  const size_t words = 4 * n + radix_bins + 2 * radix_bins + 1;
+  uint32_t* buf = nullptr;
+  if(ctx.check(cudaMalloc(&buf, sizeof(uint32_t) * words))) return MGPU_ERR_OOM;
+  const uint32_t digit0 = (uint32_t)n, one = 1;
+  uint32_t* hist = buf + 4 * n;
+  uint32_t* lookback = hist + radix_bins;
+  uint32_t* counter = lookback + 2 * radix_bins;
+  mgpu_status_t st = MGPU_OK;
+  if(ctx.check(cudaMemsetAsync(buf, 0, sizeof(uint32_t) * words, ctx.stream)) ||
+     ctx.check(cudaMemcpyAsync(hist, &digit0, 4, cudaMemcpyHostToDevice, ctx.stream)) ||
+     ctx.check(cudaMemcpyAsync(counter, &one, 4, cudaMemcpyHostToDevice, ctx.stream))) {
+    st = MGPU_ERR_CUDA;
+  } else {
+    onesweep_args<uint32_t, uint32_t> a;
+    a.keys_in = buf;
+    a.keys_out = buf + n;
+    a.vals_in = buf + 2 * n;
+    a.vals_out = buf + 3 * n;
+    a.count = n;
+    a.shift = 0;
+    a.hist = hist;
+    a.lookback = lookback;
+    a.tile_counter = counter;
+    a.error = ctx.d_error;
+    a.wait_limit = ctx.wait_limit > 0 ? ctx.wait_limit : spin_limit;
+    a.first = 1;
+    a.last = 0;
+    a.tma = 1;
+    st = ctx.launch("onesweep_pass", [&] {
+      kernel<<<1, nt, L::bytes, ctx.stream>>>(a);
+    });
+  }
+  if(ctx.check(cudaStreamSynchronize(ctx.stream)) && !st) st = MGPU_ERR_CUDA;
+  cudaFree(buf);
+  return st;
+}

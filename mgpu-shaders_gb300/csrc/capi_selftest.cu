@@ -39,3 +39,10 @@ extern "C" mgpu_status_t mgpu_selftest_bounded_wait(mgpu_context_t* c, int limit
     bounded_wait_probe<<<1, 32, 0, c->ctx.stream>>>(limit, c->ctx.d_error);
   });
 }
+
+extern "C" mgpu_status_t mgpu_set_wait_limit(mgpu_context_t* c, int polls) {
+  if(!c) return MGPU_ERR_INVALID_ARG;
+  if(polls < 0 || polls > mgpu::device::spin_limit) return MGPU_ERR_INVALID_ARG;
+  c->ctx.wait_limit = polls;
+  return MGPU_OK;
+}

@@ -9,6 +9,17 @@
 // so admitted requests overlap on the device.  Device buffers come from a
 // stream-ordered memory pool whose release threshold is the budget, so memory
 // stays resident between requests instead of returning to the driver.
+//
+// Coalescing: a small sort or scan (at most coalesce_max elements) at the
+// head of the queue is run together with the other queued small requests of
+// the same kind (same op, key type, value width, scan type and operator; up to
+// max_batch requests and batch_elems elements) as ONE segmented sort or
+// segmented scan over a packed device buffer, one request per segment: one
+// fixed launch sequence for the whole batch instead of a launch chain per
+// request.  Each request's result is the same as alone: a segment is sorted
+// in the radix order of mgpu_radix_sort and integer scans are exact, so every
+// result is byte-identical to the request run alone.  Floating-point scans,
+// larger requests and merges run alone.
 #include "capi.hxx"
 
 #include <algorithm>
@@ -27,6 +38,7 @@ typedef std::chrono::steady_clock clock_type;
 
 struct request_record {
   uint64_t id = 0;
+  uint64_t batch = 0;              // id of the coalesced batch it ran in (0: alone)
   mgpu_request_t req {};
   size_t footprint = 0;
   size_t aux_bytes = 0;
@@ -43,6 +55,36 @@ int dtype_size(mgpu_dtype_t t) {
 
 size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Coalescing limits: a request of at most coalesce_max elements joins a
+// batch; a batch holds at most max_batch requests and batch_elems elements.
+constexpr int64_t coalesce_max = int64_t(1) << 16;
+constexpr int max_batch = 512;
+constexpr int64_t batch_elems = int64_t(1) << 22;
+
+// Floating-point scans stay alone: a segmented scan adds in another order
+// than the plain scan, so their bits would depend on what they ran with.
+bool coalescible(const mgpu_request_t& r) {
+  const bool float_scan = r.op == MGPU_REQ_SCAN &&
+    (r.key_type == MGPU_F32 || r.key_type == MGPU_F64);
+  return (r.op == MGPU_REQ_SORT || r.op == MGPU_REQ_SCAN) && !float_scan && r.count > 0 &&
+         r.count <= coalesce_max;
+}
+
+bool same_kind(const mgpu_request_t& a, const mgpu_request_t& b) {
+  return a.op == b.op && a.key_type == b.key_type && a.val_bytes == b.val_bytes &&
+         (a.op != MGPU_REQ_SCAN || (a.scan_type == b.scan_type && a.op_arg == b.op_arg));
+}
+
+// Requests run together as one segmented sort or scan.
+struct batch_record {
+  uint64_t id = 0;
+  std::vector<request_record*> recs;
+  int64_t total = 0;
+  size_t footprint = 0, aux_bytes = 0;
+  int slot = -1;
+  void* dev[4] = {};               // keys, values, offsets, aux
+};
+
 }  // namespace
 
 struct mgpu_server {
@@ -52,6 +94,7 @@ struct mgpu_server {
   std::vector<mgpu_context*> slots;
   std::vector<char> slot_busy;
   int* h_err = nullptr;          // pinned: each slot's device error word after a request
+  int64_t* h_off = nullptr;      // pinned: each slot's batch offsets (max_batch + 1)
   mgpu_context* sizing = nullptr;
   cudaMemPool_t pool = nullptr;
 
@@ -59,7 +102,11 @@ struct mgpu_server {
   std::condition_variable cv_sched, cv_done;
   std::deque<uint64_t> queue;
   std::unordered_map<uint64_t, request_record*> records;
+  std::unordered_map<uint64_t, batch_record*> batches;
   std::deque<uint64_t> completions;
+  std::deque<uint64_t> batch_completions;
+  uint64_t next_batch = 1;
+  int64_t coalesced = 0, batch_launches = 0;
   size_t used = 0, peak = 0;
   int in_flight = 0;
   uint64_t next_id = 1;
@@ -104,7 +151,7 @@ struct mgpu_server {
 
   static void CUDART_CB on_complete(void* arg);
 
-  struct callback_arg { mgpu_server* server; uint64_t id; };
+  struct callback_arg { mgpu_server* server; uint64_t id; bool batch; };
 
   // Enqueues one admitted request on its slot's stream.
   mgpu_status_t launch(request_record* rec) {
@@ -178,7 +225,7 @@ struct mgpu_server {
          s) != cudaSuccess ||
        cudaMemsetAsync(c->ctx.d_error, 0, sizeof(int), s) != cudaSuccess)
       return MGPU_ERR_CUDA;
-    callback_arg* arg = new(std::nothrow) callback_arg { this, rec->id };
+    callback_arg* arg = new(std::nothrow) callback_arg { this, rec->id, false };
     if(!arg) return MGPU_ERR_OOM;
     if(cudaLaunchHostFunc(s, on_complete, arg) != cudaSuccess) { delete arg; return MGPU_ERR_CUDA; }
     return MGPU_OK;
@@ -191,6 +238,125 @@ struct mgpu_server {
       if(p) cudaFreeAsync(p, s);
       p = nullptr;
     }
+  }
+
+  // Device bytes of a batch: packed keys (and values), offsets and the
+  // segmented primitive's aux for the batch's total and segment count.
+  mgpu_status_t batch_footprint(batch_record* b) {
+    const mgpu_request_t& r = b->recs.front()->req;
+    const size_t kb = dtype_size(r.key_type), vb = r.val_bytes;
+    const int64_t n = (int64_t)b->recs.size();
+    size_t aux = 0;
+    mgpu_status_t st;
+    if(r.op == MGPU_REQ_SORT)
+      st = mgpu_segmented_sort(sizing, r.key_type, nullptr, (int)vb, nullptr, b->total, nullptr,
+        n, nullptr, &aux);
+    else
+      st = mgpu_segmented_scan(sizing, r.key_type, (mgpu_scan_type_t)r.scan_type,
+        (mgpu_op_t)r.op_arg, nullptr, nullptr, b->total, nullptr, n, nullptr, nullptr, &aux);
+    if(st) return st;
+    if(!aux) aux = 256;
+    b->aux_bytes = aux;
+    b->footprint = round256(kb * b->total) + round256(vb * b->total) +
+      round256(sizeof(int64_t) * (n + 1)) + round256(aux);
+    return MGPU_OK;
+  }
+
+  // Enqueues one admitted batch on its slot's stream: packed uploads, one
+  // segmented sort or scan, per-request downloads, one completion.
+  mgpu_status_t launch_batch(batch_record* b) {
+    mgpu_context* c = slots[b->slot];
+    cudaStream_t s = c->ctx.stream;
+    const mgpu_request_t& r0 = b->recs.front()->req;
+    const size_t kb = dtype_size(r0.key_type), vb = r0.val_bytes;
+    const int64_t n = (int64_t)b->recs.size();
+    if(cudaSetDevice(device) != cudaSuccess) return MGPU_ERR_CUDA;
+    auto alloc = [&](int i, size_t bytes) -> bool {
+      return !bytes || cudaMallocFromPoolAsync(&b->dev[i], bytes, pool, s) == cudaSuccess;
+    };
+    if(!alloc(0, kb * b->total) || !alloc(1, vb * b->total) ||
+       !alloc(2, sizeof(int64_t) * (n + 1)) || !alloc(3, b->aux_bytes))
+      return MGPU_ERR_OOM;
+    int64_t* off = h_off + (size_t)b->slot * (max_batch + 1);
+    char* dk = (char*)b->dev[0];
+    char* dv = (char*)b->dev[1];
+    off[0] = 0;
+    for(int64_t i = 0; i < n; ++i) {
+      const mgpu_request_t& r = b->recs[i]->req;
+      off[i + 1] = off[i] + r.count;
+      if(cudaMemcpyAsync(dk + kb * off[i], r.keys, kb * r.count, cudaMemcpyHostToDevice, s) !=
+           cudaSuccess ||
+         (vb && cudaMemcpyAsync(dv + vb * off[i], r.vals, vb * r.count, cudaMemcpyHostToDevice,
+           s) != cudaSuccess))
+        return MGPU_ERR_CUDA;
+    }
+    if(cudaMemcpyAsync(b->dev[2], off, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) !=
+       cudaSuccess)
+      return MGPU_ERR_CUDA;
+    size_t aux = b->aux_bytes;
+    mgpu_status_t st;
+    if(r0.op == MGPU_REQ_SORT)
+      st = mgpu_segmented_sort(c, r0.key_type, dk, (int)vb, vb ? dv : nullptr, b->total,
+        (const int64_t*)b->dev[2], n, b->dev[3], &aux);
+    else
+      st = mgpu_segmented_scan(c, r0.key_type, (mgpu_scan_type_t)r0.scan_type,
+        (mgpu_op_t)r0.op_arg, dk, dk, b->total, (const int64_t*)b->dev[2], n, nullptr,
+        b->dev[3], &aux);
+    if(st) return st;
+    for(int64_t i = 0; i < n; ++i) {
+      const mgpu_request_t& r = b->recs[i]->req;
+      if(cudaMemcpyAsync(r.out_keys, dk + kb * off[i], kb * r.count, cudaMemcpyDeviceToHost, s) !=
+           cudaSuccess ||
+         (vb && cudaMemcpyAsync(r.out_vals, dv + vb * off[i], vb * r.count,
+           cudaMemcpyDeviceToHost, s) != cudaSuccess))
+        return MGPU_ERR_CUDA;
+    }
+    release_batch(b);
+    if(cudaMemcpyAsync(h_err + b->slot, c->ctx.d_error, sizeof(int), cudaMemcpyDeviceToHost,
+         s) != cudaSuccess ||
+       cudaMemsetAsync(c->ctx.d_error, 0, sizeof(int), s) != cudaSuccess)
+      return MGPU_ERR_CUDA;
+    callback_arg* arg = new(std::nothrow) callback_arg { this, b->id, true };
+    if(!arg) return MGPU_ERR_OOM;
+    if(cudaLaunchHostFunc(s, on_complete, arg) != cudaSuccess) { delete arg; return MGPU_ERR_CUDA; }
+    return MGPU_OK;
+  }
+
+  void release_batch(batch_record* b) {
+    cudaStream_t s = slots[b->slot]->ctx.stream;
+    for(void*& p : b->dev) {
+      if(p) cudaFreeAsync(p, s);
+      p = nullptr;
+    }
+  }
+
+  // Completes every request of a batch (lock held).
+  void finish_batch_locked(batch_record* b, mgpu_status_t st) {
+    used -= b->footprint;
+    slot_busy[b->slot] = 0;
+    for(request_record* rec : b->recs) {
+      rec->footprint = 0;          // the batch held the memory
+      rec->slot = -1;
+      finish_locked(rec, st);
+    }
+    batches.erase(b->id);
+    delete b;
+  }
+
+  // Gathers the queued requests that run together with the queue head (at
+  // least the head itself).  Lock held.
+  batch_record* gather_batch() {
+    request_record* head = records[queue.front()];
+    batch_record* b = new(std::nothrow) batch_record;
+    if(!b) return nullptr;
+    for(uint64_t id : queue) {
+      request_record* rec = records[id];
+      if(!coalescible(rec->req) || !same_kind(rec->req, head->req)) continue;
+      if((int)b->recs.size() == max_batch || b->total + rec->req.count > batch_elems) break;
+      b->recs.push_back(rec);
+      b->total += rec->req.count;
+    }
+    return b;
   }
 
   void finish_locked(request_record* rec, mgpu_status_t st) {
@@ -223,13 +389,55 @@ struct mgpu_server {
         const int e = h_err[rec->slot];
         finish_locked(rec, e ? (mgpu_status_t)e : MGPU_OK);
       }
+      while(!batch_completions.empty()) {
+        batch_record* b = batches[batch_completions.front()];
+        batch_completions.pop_front();
+        const int e = h_err[b->slot];
+        finish_batch_locked(b, e ? (mgpu_status_t)e : MGPU_OK);
+      }
       if(stop && queue.empty() && in_flight == 0) break;
       bool progressed = false;
       while(!queue.empty()) {
         request_record* rec = records[queue.front()];
         int slot = -1;
         for(int i = 0; i < num_slots; ++i) if(!slot_busy[i]) { slot = i; break; }
-        if(slot < 0 || used + rec->footprint > budget) break;
+        if(slot < 0) break;
+        if(coalescible(rec->req)) {
+          batch_record* b = gather_batch();
+          if(b && b->recs.size() > 1 && !batch_footprint(b) && used + b->footprint <= budget) {
+            // Admit the batch: its requests leave the queue together.
+            b->id = next_batch++;
+            for(request_record* r : b->recs) {
+              queue.erase(std::find(queue.begin(), queue.end(), r->id));
+              r->slot = slot;
+              r->batch = b->id;
+            }
+            used += b->footprint;
+            peak = std::max(peak, used);
+            slot_busy[slot] = 1;
+            b->slot = slot;
+            in_flight += (int)b->recs.size();
+            batches[b->id] = b;
+            ++batch_launches;
+            coalesced += (int64_t)b->recs.size();
+            lk.unlock();
+            mgpu_status_t st = launch_batch(b);
+            if(st) {
+              release_batch(b);
+              cudaStreamSynchronize(slots[slot]->ctx.stream);
+            }
+            lk.lock();
+            if(st) {
+              const auto now = clock_type::now();
+              for(request_record* r : b->recs) r->finish = now;
+              finish_batch_locked(b, st);
+            }
+            progressed = true;
+            continue;
+          }
+          delete b;          // alone (or the batch does not fit yet): the single path
+        }
+        if(used + rec->footprint > budget) break;
         queue.pop_front();
         used += rec->footprint;
         peak = std::max(peak, used);
@@ -260,9 +468,17 @@ void CUDART_CB mgpu_server::on_complete(void* p) {
   mgpu_server* s = arg->server;
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->records.find(arg->id);
-    if(it != s->records.end()) it->second->finish = clock_type::now();
-    s->completions.push_back(arg->id);
+    const auto now = clock_type::now();
+    if(arg->batch) {
+      auto it = s->batches.find(arg->id);
+      if(it != s->batches.end())
+        for(request_record* rec : it->second->recs) rec->finish = now;
+      s->batch_completions.push_back(arg->id);
+    } else {
+      auto it = s->records.find(arg->id);
+      if(it != s->records.end()) it->second->finish = now;
+      s->completions.push_back(arg->id);
+    }
   }
   s->cv_sched.notify_one();
   delete arg;
@@ -302,7 +518,9 @@ mgpu_status_t mgpu_server_create(int device, size_t budget_bytes, int num_slots,
     delete s;
     return st;
   }
-  if(cudaMallocHost(&s->h_err, sizeof(int) * num_slots) != cudaSuccess) {
+  if(cudaMallocHost(&s->h_err, sizeof(int) * num_slots) != cudaSuccess ||
+     cudaMallocHost(&s->h_off, sizeof(int64_t) * (max_batch + 1) * num_slots) != cudaSuccess) {
+    if(s->h_err) cudaFreeHost(s->h_err);
     for(auto* c : s->slots) mgpu_context_destroy(c);
     mgpu_context_destroy(s->sizing);
     cudaMemPoolDestroy(s->pool);
@@ -392,6 +610,8 @@ mgpu_status_t mgpu_server_stats(mgpu_server_t* s, mgpu_server_stats_t* out) {
   out->failed = s->failed;
   out->elements = s->elements;
   out->peak_bytes = s->peak;
+  out->coalesced = s->coalesced;
+  out->batches = s->batch_launches;
   std::vector<double> l = s->latencies;
   if(!l.empty()) {
     std::sort(l.begin(), l.end());
@@ -412,6 +632,7 @@ mgpu_status_t mgpu_server_reset_stats(mgpu_server_t* s) {
   s->latencies.clear();
   s->completed = s->failed = s->elements = 0;
   s->submitted = 0;
+  s->coalesced = s->batch_launches = 0;
   s->peak = s->used;
   return MGPU_OK;
 }
@@ -425,10 +646,12 @@ mgpu_status_t mgpu_server_destroy(mgpu_server_t* s) {
   s->cv_sched.notify_one();
   if(s->scheduler.joinable()) s->scheduler.join();
   for(auto& kv : s->records) delete kv.second;
+  for(auto& kv : s->batches) delete kv.second;
   for(auto* c : s->slots) mgpu_context_destroy(c);
   if(s->sizing) mgpu_context_destroy(s->sizing);
   if(s->pool) cudaMemPoolDestroy(s->pool);
   if(s->h_err) cudaFreeHost(s->h_err);
+  if(s->h_off) cudaFreeHost(s->h_off);
   delete s;
   return MGPU_OK;
 }

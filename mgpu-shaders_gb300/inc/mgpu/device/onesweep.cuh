@@ -59,6 +59,7 @@ struct onesweep_args {
   uint32_t* lookback;        // this pass's [num_tiles][256] status words
   uint32_t* tile_counter;    // this pass's dynamic tile counter
   int* error;
+  int wait_limit = spin_limit;   // polls before a look-back or copy wait gives up
   int first;                 // convert K -> bits on load
   int last;                  // convert bits -> K on store
   int tma;                   // pointers allow 16-byte bulk copies
@@ -248,7 +249,7 @@ struct lookback_window_t {
     left -= used;
     return done;
   }
-  __device__ __forceinline__ uint32_t finish(int* error) {
+  __device__ __forceinline__ uint32_t finish(int* error, int limit) {
     uint32_t excl = 0;
     bool stalled;
     if(consume(s, excl, stalled)) return excl;
@@ -256,7 +257,7 @@ struct lookback_window_t {
     while(true) {
       if(stalled) {
         ++spins;
-        if(spins >= spin_limit ||
+        if(spins >= limit ||
            (0 == (spins & (spin_poll_error - 1)) && error_raised(error))) {
           raise_error(error, err_lookback_timeout);
           return excl;
@@ -370,11 +371,11 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     // completion makes the copied bytes visible to warp 0, and the CTA
     // barrier passes that on to every thread.
     bool ok = true;
-    if(bulk_k && warp == 0) ok = mbar_wait_bounded(bar, 0, a.error);
+    if(bulk_k && warp == 0) ok = mbar_wait_bounded(bar, 0, a.error, a.wait_limit);
     if(__syncthreads_or(!ok)) {
       // The copy did not complete in time: wait once more (bounded) so no
       // bulk copy is still writing this CTA's shared memory, then leave.
-      if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
+      if(warp == 0) mbar_wait_bounded(bar, 0, a.error, a.wait_limit);
       return;
     }
   }
@@ -499,7 +500,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   if(tid < radix_bins) {
     uint32_t excl = 0;
     if(tile > 0) {
-      excl = lbw.finish(a.error);
+      excl = lbw.finish(a.error, a.wait_limit);
       st_relaxed(&t.lb_row[tid], lb_inc | (excl + valid_cnt));
     }
     gbase[tid] = (int)(glob_start + excl - tile_start);
@@ -547,9 +548,9 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     V* const av = (V*)A + voff + warp_base + lane;     // this thread's staged values
     // The sorted keys must have left B, and (when copied) the values arrived.
     bool ok = true;
-    if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error);
+    if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error, a.wait_limit);
     if(__syncthreads_or(!ok)) {
-      if(warp == 0) mbar_wait_bounded(bar, vparity, a.error);
+      if(warp == 0) mbar_wait_bounded(bar, vparity, a.error, a.wait_limit);
       return;
     }
     if(vfill < valid) {

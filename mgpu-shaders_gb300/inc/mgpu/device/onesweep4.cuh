@@ -107,9 +107,9 @@ __device__ __forceinline__ void onesweep4_tile(const onesweep_args<K, V>& a,
   }
   {
     bool ok = true;
-    if(bulk_k && warp == 0) ok = mbar_wait_bounded(bar, 0, a.error);
+    if(bulk_k && warp == 0) ok = mbar_wait_bounded(bar, 0, a.error, a.wait_limit);
     if(__syncthreads_or(!ok)) {
-      if(warp == 0) mbar_wait_bounded(bar, 0, a.error);
+      if(warp == 0) mbar_wait_bounded(bar, 0, a.error, a.wait_limit);
       return;
     }
   }
@@ -201,7 +201,7 @@ __device__ __forceinline__ void onesweep4_tile(const onesweep_args<K, V>& a,
   if(warp == 0 && lane < BINS) {
     uint32_t excl = 0;
     if(tile > 0) {
-      excl = lbw.finish(a.error);
+      excl = lbw.finish(a.error, a.wait_limit);
       st_relaxed(&t.lb_row[lane], lb_inc | (excl + valid_cnt));
     }
     gbase[lane] = (int)(glob_start + excl - tile_start);
@@ -242,9 +242,9 @@ __device__ __forceinline__ void onesweep4_tile(const onesweep_args<K, V>& a,
   if constexpr(HAS_V) {
     V* const av = (V*)A + warp_base + lane;
     bool ok = true;
-    if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error);
+    if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error, a.wait_limit);
     if(__syncthreads_or(!ok)) {
-      if(warp == 0) mbar_wait_bounded(bar, vparity, a.error);
+      if(warp == 0) mbar_wait_bounded(bar, vparity, a.error, a.wait_limit);
       return;
     }
     if(vfill < valid) {

@@ -203,6 +203,9 @@ struct context_t {
   cudaStream_t stream = nullptr;
   cudaStream_t owned_stream = nullptr;
   int* d_error = nullptr;
+  // Polls before a radix pass's look-back or copy wait gives up and raises
+  // MGPU_ERR_LOOKBACK_TIMEOUT; 0 keeps the library's limit (seconds).
+  int wait_limit = 0;
   status_t init_status = MGPU_OK;
   std::string last_error;
 

@@ -150,6 +150,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     a.lookback = lookback + (size_t)p * num_tiles * bins;
     a.tile_counter = counters + p;
     a.error = ctx.d_error;
+    a.wait_limit = ctx.wait_limit > 0 ? ctx.wait_limit : spin_limit;
     a.first = p == 0;
     a.last = p == passes - 1;
     a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));

@@ -116,6 +116,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
     a.lookback = nullptr;
     a.tile_counter = s.counters + sc_pass_tiles + p;
     a.error = ctx.d_error;
+    a.wait_limit = ctx.wait_limit > 0 ? ctx.wait_limit : spin_limit;
     a.first = p == 0;
     a.last = p == PASSES - 1;
     a.tma = aligned16_host(a.keys_in) && (!has_values || aligned16_host(a.vals_in));

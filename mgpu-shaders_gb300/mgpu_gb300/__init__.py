@@ -127,6 +127,17 @@ class Context:
         MgpuError with status 3 (a bounded wait gave up)."""
         self._check(lib().mgpu_selftest_bounded_wait(self._h, limit))
 
+    def set_wait_limit(self, polls):
+        """Polls before a radix pass's look-back or copy wait gives up (0:
+        the library's limit)."""
+        self._check(lib().mgpu_set_wait_limit(self._h, polls))
+
+    def selftest_lookback_timeout(self):
+        """Runs the production radix pass on a tile whose look-back
+        predecessor never publishes (synchronises); the next synchronize()
+        raises MgpuError with status 3."""
+        self._check(lib().mgpu_selftest_lookback_timeout(self._h))
+
     # --- launch-shape tuning ---
     def tuning_variants(self, primitive, key_dtype):
         buf = ctypes.create_string_buffer(512)
@@ -332,7 +343,8 @@ class ServerStats(ctypes.Structure):
                 ("failed", ctypes.c_int64), ("elements", ctypes.c_int64),
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
                 ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
-                ("peak_bytes", ctypes.c_size_t)]
+                ("peak_bytes", ctypes.c_size_t), ("coalesced", ctypes.c_int64),
+                ("batches", ctypes.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

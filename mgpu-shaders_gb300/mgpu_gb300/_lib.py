@@ -79,6 +79,8 @@ _SIGS = {
     "mgpu_profile_read": ([_VP, _VP, ctypes.c_size_t, _VP, _VP, _I32, _VP], _I32),
     "mgpu_launch_count": ([_VP], _I64),
     "mgpu_selftest_bounded_wait": ([_VP, _I32], _I32),
+    "mgpu_selftest_lookback_timeout": ([_VP], _I32),
+    "mgpu_set_wait_limit": ([_VP, _I32], _I32),
     "mgpu_scan_noalloc": ([_VP, _I32, _I32, _I32, _VP, _VP, _I64, _VP, _VP], _I32),
     "mgpu_scan_noalloc_status": ([_VP], _I32),
     "mgpu_selftest_scan_noalloc_wait": ([_VP, _I32], _I32),

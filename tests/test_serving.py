@@ -167,3 +167,128 @@ def test_latency_record(server_cls, rng):
     srv.reset_stats()
     assert srv.stats()["completed"] == 0
     srv.close()
+
+
+def bench_mix_requests(rng, n_req, max_log2):
+    """The serving benchmark's mix, bounded for test time: sort / merge / scan
+    in turn, sizes log-uniform in [2^10, 2^max_log2], keys u32 / u64 / f32 at
+    50/25/25 %, sorts and merges carrying u32 values, integer scans exclusive
+    and f32 scans inclusive."""
+    reqs = []
+    for i in range(n_req):
+        n = int(2 ** rng.uniform(10, max_log2))
+        kt = [np.uint32, np.uint32, np.uint64, np.float32][rng.integers(0, 4)]
+        kind = ("sort", "merge", "scan")[i % 3]
+        if kind == "sort":
+            reqs.append(("sort", gen_keys(rng, n, kt), np.arange(n, dtype=np.uint32)))
+        elif kind == "merge":
+            na = n // 2
+            a, b = np.sort(gen_keys(rng, na, kt)), np.sort(gen_keys(rng, n - na, kt))
+            reqs.append(("merge", a, np.arange(na, dtype=np.uint32), b,
+                         np.arange(n - na, dtype=np.uint32) + na))
+        else:
+            x = rng.standard_normal(n).astype(np.float32) if kt == np.float32 else \
+                rng.integers(0, 1 << 20, n).astype(kt)
+            reqs.append(("scan", x, "inc" if kt == np.float32 else "exc"))
+    return reqs
+
+
+def run_alone(server_cls, reqs):
+    srv = server_cls(budget_bytes=1 << 31, num_slots=1)
+    outs = []
+    for r in reqs:
+        rid, o = submit(srv, r)
+        srv.wait(rid)
+        outs.append(o)
+    assert srv.stats()["coalesced"] == 0
+    srv.close()
+    return outs
+
+
+def test_bench_mix_equals_alone(server_cls, oracle, rng):
+    # The benchmark's key types and operations at sizes up to 2^22, all queued
+    # at once: every result is byte-identical to the request served alone, and
+    # to the oracle.  f32 scans are checked against the float64 oracle within
+    # the bound of the scan tests: the scan's look-back adds tile aggregates
+    # in an order that depends on timing, so their last bits vary by run.
+    reqs = bench_mix_requests(rng, 60, 22)
+    alone = run_alone(server_cls, reqs)
+    srv = server_cls(budget_bytes=1 << 30, num_slots=4)
+    pending = [submit(srv, r) for r in reqs]
+    for rid, _ in pending:
+        srv.wait(rid)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    for r, a, (_, m) in zip(reqs, alone, pending):
+        if r[0] == "scan" and r[1].dtype == np.float32:
+            ref = np.cumsum(r[1].astype(np.float64))
+            tol = 1e-4 * np.abs(r[1]).astype(np.float64).sum() + 1e-6
+            assert np.max(np.abs(m[0] - ref)) <= tol
+            assert np.max(np.abs(a[0] - ref)) <= tol
+        else:
+            assert same(a[0], m[0]) and same(a[1], m[1]), (r[0], r[1].dtype, r[1].size)
+            ek, ev = expected(oracle, r)
+            assert same(ek, m[0]) and same(ev, m[1]), r[0]
+
+
+def small_requests(rng, n_req):
+    """Small sorts (keys only and key-value) and integer scans of a few kinds,
+    interleaved, sizes 1 .. 2^16 (the coalescing limit)."""
+    reqs = []
+    for i in range(n_req):
+        n = int(2 ** rng.uniform(0, 16))
+        if i % 7 == 6:
+            n = 1 << 16
+        c = i % 4
+        if c == 0:
+            reqs.append(("sort", gen_keys(rng, n, np.uint32), np.arange(n, dtype=np.uint32)))
+        elif c == 1:
+            reqs.append(("sort", gen_keys(rng, n, np.float32), None))
+        elif c == 2:
+            reqs.append(("scan", rng.integers(0, 1 << 20, n).astype(np.int32), "exc"))
+        else:
+            reqs.append(("scan", rng.integers(0, 1 << 40, n).astype(np.uint64), "inc"))
+    return reqs
+
+
+def test_small_requests_coalesce(server_cls, oracle, rng):
+    # 200 small requests queued behind one large sort that holds the only
+    # slot: the queue fills, and the small ones run in coalesced batches (one
+    # segmented sort or scan per batch) with the same bytes as alone.
+    reqs = small_requests(rng, 200)
+    alone = run_alone(server_cls, reqs)
+    srv = server_cls(budget_bytes=1 << 30, num_slots=1)
+    big = gen_keys(rng, 1 << 22, np.uint32)
+    big_out = np.empty_like(big)
+    first = srv.submit_sort(big, None, big_out, None)
+    pending = [submit(srv, r) for r in reqs]
+    srv.wait(first)
+    for rid, _ in pending:
+        srv.wait(rid)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs) + 1 and st["failed"] == 0
+    assert st["coalesced"] >= len(reqs) // 2 and 0 < st["batches"] < st["coalesced"]
+    assert np.array_equal(big_out, np.sort(big))
+    for r, a, (_, m) in zip(reqs, alone, pending):
+        assert same(a[0], m[0]) and same(a[1], m[1]), (r[0], r[1].dtype, r[1].size)
+        ek, ev = expected(oracle, r)
+        assert same(ek, m[0]) and same(ev, m[1]), r[0]
+
+
+def test_coalescing_respects_budget(server_cls, oracle, rng):
+    # A budget that holds only part of a batch: batches shrink to fit or the
+    # requests run alone; nothing exceeds the budget and every result is right.
+    reqs = small_requests(rng, 64)
+    srv = server_cls(budget_bytes=2 << 20, num_slots=2)
+    pending = [submit(srv, r) for r in reqs]
+    for rid, _ in pending:
+        srv.wait(rid)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["peak_bytes"] <= 2 << 20
+    for r, (_, m) in zip(reqs, pending):
+        ek, ev = expected(oracle, r)
+        assert same(ek, m[0]) and same(ev, m[1]), r[0]
