@@ -528,10 +528,11 @@ def wl_segsort(args, mg, torch):
     ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
     gk, gv = wk.numpy(), wv.numpy()
     checks = segmented_sort_checks(keys, off, gk, gv)
-    # Segments of up to one 5120-key tile sort inside seg_small_sort; larger
-    # ones go through seg_onesweep_pass, one launch per digit.
+    # Segments of up to one 5376-key tile (256 threads x 21 keys) are merge-
+    # sorted inside seg_small_sort; larger ones go through seg_onesweep_pass,
+    # one launch per digit.
     seg_lens = np.diff(off)
-    small_keys = int(seg_lens[seg_lens <= 5120].sum())
+    small_keys = int(seg_lens[seg_lens <= 5376].sum())
     roof, kernels = _roofline(ctx, run, restore, 3,
                               {"seg_small_sort": 16 * small_keys,
                                "seg_onesweep_pass": 16 * (n - small_keys)})

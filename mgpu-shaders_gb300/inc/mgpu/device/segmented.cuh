@@ -20,6 +20,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "merge.cuh"
 #include "onesweep.cuh"
 #include "scan.cuh"
 
@@ -103,66 +104,82 @@ __device__ __forceinline__ void warp_rank_sort(K* keys, V* vals, int n) {
 
 // Stable LSD radix sort (8-bit digits) of n <= 32 * W * ITEMS keys held in a
 // shared-memory slice, by a group of W warps.  gtid is the thread's index in
-// the group; hist has W * 256 words; tmp has W words.  Keys are radix bits.
-// The ceil(n / 32) rows of 32 keys are spread evenly over the warps (warp w
-// ranks rows [w * rpw, (w + 1) * rpw), so a short segment does not wait on
-// one warp's long chain); rows past n are skipped (the last partial row pads
-// with all-ones keys, which rank after every real key and land past n).
-// Peers come from one ballot per digit bit.
+// the group; mwords has W * 512 words (each warp's 256 64-bit match words);
+// tmp has W words.  Keys are radix bits.  The ceil(n / 32) rows of 32 keys are
+// spread evenly over the warps (warp w ranks rows [w * rpw, (w + 1) * rpw), so
+// a short segment does not wait on one warp's long chain); rows past n are
+// skipped (the last partial row pads with all-ones keys, which rank after
+// every real key and land past n).
+// Ranking as in the onesweep pass: per digit one 64-bit word holds the row's
+// peer mask (each lane ORs its bit in) and the warp's running count; a lane
+// reads both in one load and the lowest peer writes back the advanced count
+// with a cleared mask -- three shared-memory operations per key and no ballot
+// chain, which keeps the kernel off the integer pipe's limit.  Digits with
+// bit 4 set keep the mask in the upper half, so the masks of any 32 digits
+// spread over the 32 banks.  Ranks (< 2^16) are kept as packed pairs.
 template<int W, int ITEMS, typename U, typename V>
-__device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* hist,
+__device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* mwords,
   uint32_t* tmp, int passes, int gtid) {
   constexpr bool HAS_V = !std::is_same<V, no_values>::value;
   constexpr int G = 32 * W;
   constexpr int DPT = G >= radix_bins ? 1 : radix_bins / G;   // digits per thread
   static_assert(G >= radix_bins ? G % radix_bins == 0 : radix_bins % G == 0, "group size");
+  static_assert(ITEMS % 2 == 0 && 32 * W * ITEMS <= 65536, "ranks are packed 16-bit pairs");
   const int lane = gtid & 31, gw = gtid >> 5;
   const int rpw = min(ITEMS, (((n + 31) >> 5) + W - 1) / W);         // rows per warp
   const int warp_base = gw * 32 * rpw;
   const int rem = n - warp_base - lane;
   const int rows = min(rpw, max(0, (n - warp_base + 31) >> 5));      // warp-uniform
   const uint32_t lt_mask = lanemask_lt();
+  const uint32_t lane_bit = 1u << lane;
+  uint32_t* mw = mwords + gw * 2 * radix_bins;
+  // Word holding the count (after the scan: the offset) of digit d.
+  auto cslot = [](uint32_t d) -> uint32_t { return 2 * d + 1 - ((d >> 4) & 1); };
   auto gsync = [] { if(W == 1) __syncwarp(); else __syncthreads(); };
   for(int pass = 0; pass < passes; ++pass) {
     const int shift = 8 * pass;
-    for(int i = gtid; i < W * radix_bins; i += G) hist[i] = 0;
+    for(int i = gtid; i < W * 2 * radix_bins / 4; i += G)
+      reinterpret_cast<uint4*>(mwords)[i] = make_uint4(0, 0, 0, 0);
     U k[ITEMS];
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i)
       if(i < rows) k[i] = 32 * i < rem ? ks[warp_base + 32 * i + lane] : ~(U)0;
     gsync();
-    uint32_t r[ITEMS];
-    uint32_t* wh = hist + gw * radix_bins;
+    uint32_t rp[ITEMS / 2];
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
       if(i < rows) {
         const uint32_t d = extract_digit(k[i], shift, 8);
-        uint32_t peers = 0xffffffffu;
-#pragma unroll
-        for(int b = 0; b < 8; ++b) {
-          const bool bit = (d >> b) & 1u;
-          const uint32_t m = __ballot_sync(0xffffffffu, bit);
-          peers &= bit ? m : ~m;
-        }
+        const uint32_t hi = (d >> 4) & 1;
+        atomicOr(&mw[2 * d + hi], lane_bit);
+        __syncwarp();
+        const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
+        __syncwarp();
+        const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
         const uint32_t below = peers & lt_mask;
-        const uint32_t cnt = wh[d];
+        if(!below) {
+          const uint32_t next = cnt + __popc(peers);
+          *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
+        }
         __syncwarp();
-        if(!below) wh[d] = cnt + __popc(peers);
-        __syncwarp();
-        r[i] = cnt + __popc(below);
+        const uint32_t rank = cnt + __popc(below);
+        if(i & 1) rp[i >> 1] |= rank << 16;
+        else rp[i >> 1] = rank;
       }
     }
     gsync();
+    // Per digit: the warps' counts -> exclusive offsets over warps, in place.
     uint32_t tot[DPT];
     uint32_t sum = 0;
 #pragma unroll
     for(int j = 0; j < DPT; ++j) {
-      int d = gtid * DPT + j;
+      const int d = gtid * DPT + j;
       uint32_t t = 0;
       if(d < radix_bins) {
+        const uint32_t c0 = cslot(d);
         for(int w = 0; w < W; ++w) {
-          uint32_t c = hist[w * radix_bins + d];
-          hist[w * radix_bins + d] = t;
+          const uint32_t c = mwords[w * 2 * radix_bins + c0];
+          mwords[w * 2 * radix_bins + c0] = t;
           t += c;
         }
       }
@@ -173,7 +190,7 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
     uint32_t inc = sum;
 #pragma unroll
     for(int off = 1; off < 32; off <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
       if(lane >= off) inc += y;
     }
     uint32_t excl = inc - sum;
@@ -184,9 +201,11 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
     }
 #pragma unroll
     for(int j = 0; j < DPT; ++j) {
-      int d = gtid * DPT + j;
-      if(d < radix_bins)
-        for(int w = 0; w < W; ++w) hist[w * radix_bins + d] += excl;
+      const int d = gtid * DPT + j;
+      if(d < radix_bins) {
+        const uint32_t c0 = cslot(d);
+        for(int w = 0; w < W; ++w) mwords[w * 2 * radix_bins + c0] += excl;
+      }
       excl += tot[j];
     }
     gsync();
@@ -195,8 +214,10 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
       if(i < rows) {
-        r[i] += wh[extract_digit(k[i], shift, 8)];
-        ks[r[i]] = k[i];
+        const uint32_t sh = (i & 1) * 16;
+        const uint32_t r = ((rp[i >> 1] >> sh) & 0xffffu) + mw[cslot(extract_digit(k[i], shift, 8))];
+        rp[i >> 1] = (rp[i >> 1] & ~(0xffffu << sh)) | (r << sh);
+        ks[r] = k[i];
       }
     }
     if constexpr(HAS_V) {
@@ -207,13 +228,96 @@ __device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* 
       gsync();
 #pragma unroll
       for(int i = 0; i < ITEMS; ++i)
-        if(i < rows) vs[r[i]] = v[i];
+        if(i < rows) vs[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = v[i];
     }
     gsync();
   }
 }
 
-template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS>
+// Stable merge sort of n <= 32 * W * VT keys (radix bits) and values held in
+// shared memory, by a group of W warps (gtid: the thread's index in the
+// group).  Each thread sorts VT consecutive items in registers by odd-even
+// transposition (only adjacent, strictly descending pairs swap, so equal keys
+// keep their order; positions past n hold all-ones bits, which never move
+// before a real key), then merge passes through shared memory double the
+// sorted runs until one run covers n (merge path with A first on ties).  The
+// result is the stable order by radix bits, the order of the LSD radix sort.
+// About 2 + 3 log2(n / VT) instructions per key against the radix sort's four
+// full passes: the choice for segments of a few thousand keys.
+template<int W, int VT, typename U, typename V>
+__device__ __forceinline__ void group_merge_sort(U* sk, V* sv, int n, int gtid) {
+  constexpr bool HAS_V = !std::is_same<V, no_values>::value;
+  constexpr int G = 32 * W;
+  typedef typename std::conditional<HAS_V, V, char>::type VR;
+  auto gsync = [] { if(W == 1) __syncwarp(); else __syncthreads(); };
+  const int first = VT * gtid;
+  U k[VT];
+  VR v[VT];
+#pragma unroll
+  for(int i = 0; i < VT; ++i) {
+    const int j = first + i;
+    k[i] = j < n ? sk[j] : ~(U)0;
+    if constexpr(HAS_V) v[i] = j < n ? sv[j] : V();
+  }
+#pragma unroll
+  for(int I = 0; I < VT; ++I) {
+#pragma unroll
+    for(int i = 1 & I; i < VT - 1; i += 2) {
+      if(k[i + 1] < k[i]) {
+        const U t = k[i]; k[i] = k[i + 1]; k[i + 1] = t;
+        if constexpr(HAS_V) { const VR u = v[i]; v[i] = v[i + 1]; v[i + 1] = u; }
+      }
+    }
+  }
+#pragma unroll 1
+  for(int coop = 2; coop <= G && VT * (coop >> 1) < n; coop <<= 1) {
+    gsync();                           // readers of the previous pass are done
+#pragma unroll
+    for(int i = 0; i < VT; ++i) {
+      if(first + i < n) {
+        sk[first + i] = k[i];
+        if constexpr(HAS_V) sv[first + i] = v[i];
+      }
+    }
+    gsync();
+    if(first < n) {
+      const int start = VT * (gtid & ~(coop - 1));
+      const int half = VT * (coop >> 1);
+      const int a_begin = start, a_end = min(start + half, n);
+      const int b_begin = a_end, b_end = min(start + 2 * half, n);
+      const int a_cnt = a_end - a_begin, b_cnt = b_end - b_begin;
+      const int diag = min(first - start, a_cnt + b_cnt);
+      const U* A = sk + a_begin;
+      const U* B = sk + b_begin;
+      int ai = merge_path(A, a_cnt, B, b_cnt, diag, less_t<U>());
+      int bi = diag - ai;
+      U ak = A[min(ai, max(a_cnt - 1, 0))];
+      U bk = B[min(bi, max(b_cnt - 1, 0))];
+#pragma unroll
+      for(int i = 0; i < VT; ++i) {
+        const bool take_a = bi >= b_cnt || (ai < a_cnt && !(bk < ak));
+        k[i] = take_a ? ak : bk;
+        if constexpr(HAS_V) v[i] = sv[take_a ? a_begin + ai : b_begin + bi];
+        if(take_a) { ++ai; ak = A[min(ai, max(a_cnt - 1, 0))]; }
+        else { ++bi; bk = B[min(bi, max(b_cnt - 1, 0))]; }
+      }
+    }
+  }
+  gsync();
+#pragma unroll
+  for(int i = 0; i < VT; ++i) {
+    if(first + i < n) {
+      sk[first + i] = k[i];
+      if constexpr(HAS_V) sv[first + i] = v[i];
+    }
+  }
+  gsync();
+}
+
+// Shared memory of the in-CTA sorts: the tile's keys (radix bits) and values,
+// then (radix sort only, MWORDS) each warp's 256 64-bit match words, scan
+// scratch and a work-item slot.
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, bool MWORDS = true>
 struct seg_small_layout {
   typedef typename radix_key<K>::bits_t U;
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
@@ -223,7 +327,7 @@ struct seg_small_layout {
   static constexpr size_t keys_off = 0;
   static constexpr size_t vals_off = sizeof(U) * tile;
   static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
-  static constexpr size_t tmp_off = hist_off + sizeof(uint32_t) * warps * radix_bins;
+  static constexpr size_t tmp_off = hist_off + (MWORDS ? sizeof(uint32_t) * warps * 2 * radix_bins : 0);
   static constexpr size_t misc_off = tmp_off + sizeof(uint32_t) * 32;
   static constexpr size_t bytes = misc_off + 16;
   static_assert(warps * slice <= tile, "warp slices fit in the tile buffers");
@@ -286,14 +390,12 @@ __device__ __forceinline__ void seg_stage_in(const K* keys, const V* vals, int n
 template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES, int MINB = 1>
 __global__ void __launch_bounds__(NT, MINB)
 seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
-  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS, false> L;
   typedef typename L::U U;
   constexpr bool HAS_V = L::has_values;
   extern __shared__ __align__(16) unsigned char smem[];
   U* ks = (U*)(smem + L::keys_off);
   V* vs = (V*)(smem + L::vals_off);
-  uint32_t* hist = (uint32_t*)(smem + L::hist_off);
-  uint32_t* tmp = (uint32_t*)(smem + L::tmp_off);
   int* s_item = (int*)(smem + L::misc_off);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -310,7 +412,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int n = (int)(offsets[seg + 1] - b);
     seg_stage_in<NT>(keys + b, HAS_V ? vals + b : vals, n, ks, vs, tid);
     __syncthreads();
-    group_radix_sort<NT / 32, ITEMS>(ks, vs, n, hist, tmp, PASSES, tid);
+    group_merge_sort<NT / 32, ITEMS>(ks, vs, n, tid);
     for(int i = tid; i < n; i += NT) {
       keys[b + i] = radix_key<K>::from_bits(ks[i]);
       if constexpr(HAS_V) vals[b + i] = vs[i];
@@ -322,7 +424,6 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
   const uint32_t num_slice = s.counters[sc_slice];
   U* wks = ks + warp * L::slice;
   V* wvs = vs + warp * L::slice;
-  uint32_t* wh = hist + warp * radix_bins;
   while(true) {
     int item = 0;
     if(lane == 0) item = (int)atomicAdd(&s.counters[sc_next_slice], 1u);
@@ -333,7 +434,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int n = (int)(offsets[seg + 1] - b);
     seg_stage_in<32>(keys + b, HAS_V ? vals + b : vals, n, wks, wvs, lane);
     __syncwarp();
-    group_radix_sort<1, SLICE_ITEMS>(wks, wvs, n, wh, nullptr, PASSES, lane);
+    group_merge_sort<1, SLICE_ITEMS>(wks, wvs, n, lane);
     for(int i = lane; i < n; i += 32) {
       keys[b + i] = radix_key<K>::from_bits(wks[i]);
       if constexpr(HAS_V) vals[b + i] = wvs[i];

@@ -20,6 +20,18 @@
 namespace mgpu {
 namespace gb300 {
 
+// Segments of at most one small-sort tile (nt x vt keys) are merge-sorted in
+// shared memory by one CTA (one warp for those of at most 32 x vt keys).  vt is
+// odd so that threads' runs of vt items start in distinct banks (an even vt
+// shares banks: 16 keys per thread made the kernel 1.6x slower than 21); four
+// CTAs per SM at 64 registers.  By the width of the staged elements (the
+// wider of key and value), as the onesweep shapes.  Measured on 10^5 lognormal segments (u32 keys
+// + values): vt 21 -> 4.47 ms per batch, 19 -> 4.49, 17 -> 4.54, 15 -> 4.62;
+// three CTAs per SM at vt 21 -> 4.60.
+template<int elem_bytes> struct seg_small_tuning;
+template<> struct seg_small_tuning<4> { enum { nt = 256, vt = 21, min_blocks = 4 }; };
+template<> struct seg_small_tuning<8> { enum { nt = 256, vt = 13, min_blocks = 4 }; };
+
 template<typename K, typename V>
 status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys, V* vals,
   int64_t count, const int64_t* offsets, int64_t num_segments) {
@@ -27,18 +39,18 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   typedef typename radix_key<K>::bits_t U;
   // Segments of at most one CTA tile sort in the small-segment kernel; larger
   // ones go through onesweep passes over tiles of the plain sort's shape.
-  typedef cta_sort_tuning<sizeof(K)> T;
+  typedef seg_small_tuning<radix_elem_bytes<K, V>()> T;
   constexpr int NT = T::nt, ITEMS = T::vt;
   constexpr int TILE = NT * ITEMS;
   typedef radix_tuning<radix_elem_bytes<K, V>()> OT;
   constexpr int ONT = OT::nt, OITEMS = OT::vt, MINB = OT::min_blocks;
   constexpr int OTILE = ONT * OITEMS;
   constexpr int SLICE_ITEMS = ITEMS;
-  constexpr int SMALL_MINB = 3;   // 3 CTAs/SM: 1.66 ms against 1.91 ms at 2 (108 registers)
+  constexpr int SMALL_MINB = T::min_blocks;
   constexpr int SLICE = 32 * SLICE_ITEMS;
   constexpr int PASSES = sizeof(K);
   constexpr bool has_values = !std::is_same<V, no_values>::value;
-  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> SL;
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS, false> SL;
   typedef onesweep_layout<K, V, ONT, OITEMS> OL;
   if(count < 0 || num_segments < 0 || count > radix_max_count || num_segments > INT32_MAX)
     return MGPU_ERR_INVALID_ARG;
