@@ -950,6 +950,54 @@ SECONDARY = ["radix_u64", "radix_f32", "radix_f32_normal", "mergesort", "merge",
              "scan_f32", "segsort", "segscan"]
 
 
+def cub_comparator(torch, keys_h, vals_h, steps, warmup):
+    """NVIDIA CUB's DeviceRadixSort::SortPairs on the headline input, timed
+    like the library's sort (CUDA events per step, a fresh unsorted copy
+    restored outside the events), for information only: bench_cub.cu is
+    compiled on first use and is not part of the library.  Its output must
+    equal the library's (both are the stable sort by radix bits)."""
+    import ctypes
+    import subprocess
+    src = os.path.join(REPO, "bench_cub.cu")
+    out_dir = os.path.join(REPO, "build", "bench_cub")
+    so = os.path.join(out_dir, "libbench_cub.so")
+    if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+        os.makedirs(out_dir, exist_ok=True)
+        subprocess.check_call(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                               "-std=c++17", "-shared", "-Xcompiler", "-fPIC", src, "-o", so])
+    lib = ctypes.CDLL(so)
+    lib.bench_cub_sort_pairs_u32.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)] + \
+        [ctypes.c_void_p] * 4 + [ctypes.c_int64, ctypes.c_void_p]
+    n = keys_h.size
+    pk = torch.from_numpy(keys_h.view(np.int32)).cuda()
+    pv = torch.from_numpy(vals_h.view(np.int32)).cuda()
+    wk, wv = torch.empty_like(pk), torch.empty_like(pv)
+    ok, ov = torch.empty_like(pk), torch.empty_like(pv)
+    stream = torch.cuda.current_stream()
+    tb = ctypes.c_size_t(0)
+    args_ = lambda t: (t, ctypes.byref(tb), wk.data_ptr(), ok.data_ptr(), wv.data_ptr(),  # noqa
+                       ov.data_ptr(), n, stream.cuda_stream)
+    if lib.bench_cub_sort_pairs_u32(*args_(None)):
+        raise RuntimeError("CUB sizing call failed")
+    temp = torch.empty(tb.value, dtype=torch.uint8, device="cuda")
+    ms = []
+    for i in range(warmup + steps):
+        wk.copy_(pk)
+        wv.copy_(pv)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if lib.bench_cub_sort_pairs_u32(*args_(temp.data_ptr())):
+            raise RuntimeError("CUB SortPairs failed")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i >= warmup:
+            ms.append(e0.elapsed_time(e1))
+    t = sum(ms) / len(ms)
+    gk = ok.cpu().numpy().view(np.uint32)
+    gv = ov.cpu().numpy().view(np.uint32)
+    return t, gk, gv
+
+
 def run_secondary(args, mg, torch):
     """Short timed runs (same timing rules) of every other benchmark
     configuration, summarised for the headline line."""
@@ -995,6 +1043,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the short runs of the other configurations")
     ap.add_argument("--secondary-steps", type=int, default=10)
+    ap.add_argument("--no-comparator", action="store_true",
+                    help="skip the informational CUB radix sort on the headline input")
     ap.add_argument("--seg-count", type=int, default=100_000,
                     help="segsort/segscan: number of lognormal segments")
     ap.add_argument("--no-plain", action="store_true",
@@ -1182,6 +1232,17 @@ def main():
     del copies, bufs, pristine_k, pristine_v, aux_t, outs, hk, hv
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
+    if rank == 0 and not args.no_comparator:
+        # NVIDIA's own onesweep radix sort (CUB) on the same input and GPU.
+        cub_ms, ck, cv = cub_comparator(torch, keys_h, vals_h, min(steps, 10), warmup)
+        line["comparator"] = {
+            "impl": "cub::DeviceRadixSort::SortPairs (CUDA toolkit CCCL), same input",
+            "ms_per_step": cub_ms, "value": n / (cub_ms * 1e-3) / 1e6, "unit": "Mkeys/s",
+            "frac_of_peak_at_68B_per_key": ALG_BYTES_PER_KEY * n / (cub_ms * 1e-3) / 1e9 / peak,
+            "library_speedup": cub_ms / ms,
+            "same_output": bool(np.array_equal(ck, gk) and np.array_equal(cv, gv))}
+        del ck, cv
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_secondary and args.n == N_KEYS:
         line["secondary"] = run_secondary(args, mg, torch)
     if rank == 0 and not args.no_cpu_baseline:

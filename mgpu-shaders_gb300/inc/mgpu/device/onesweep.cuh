@@ -151,7 +151,22 @@ radix_histogram(const K* keys, int64_t count, uint32_t* hist, int vectorised,
   constexpr int per_vec = 16 / sizeof(K);
   int64_t num_vec = vectorised ? count / per_vec : 0;
   const uint4* kv = (const uint4*)keys;
-  for(int64_t i = gid; i < num_vec; i += stride) {
+  // Four 16-byte loads in flight per thread before their keys are counted:
+  // with one, the kernel waited on memory latency (45 % of DRAM peak).
+  constexpr int UNROLL = 4;
+  int64_t i = gid;
+  for(; i + (UNROLL - 1) * stride < num_vec; i += UNROLL * stride) {
+    uint4 v[UNROLL];
+#pragma unroll
+    for(int u = 0; u < UNROLL; ++u) v[u] = __ldcs(kv + i + u * stride);
+#pragma unroll
+    for(int u = 0; u < UNROLL; ++u) {
+      const K* e = (const K*)&v[u];
+#pragma unroll
+      for(int j = 0; j < per_vec; ++j) count_key(e[j]);
+    }
+  }
+  for(; i < num_vec; i += stride) {
     uint4 v = kv[i];
     const K* e = (const K*)&v;
 #pragma unroll

@@ -464,8 +464,14 @@ template<typename K, int NT, int TILE, int PASSES>
 __global__ void __launch_bounds__(NT)
 seg_histogram(const K* keys, const int64_t* offsets, seg_state_t s) {
   typedef typename radix_key<K>::bits_t U;
-  __shared__ uint32_t sh[PASSES * radix_bins];
+  // Each bin has COPIES copies and lane l counts into copy l % COPIES, which
+  // spreads a warp's atomics on equal or bank-sharing bins (one copy gave 68 %
+  // bank conflicts); 32 KB either way.
+  constexpr int COPIES = PASSES <= 4 ? 8 : 4;
+  constexpr int BINS = PASSES * radix_bins;
+  __shared__ uint32_t sh[BINS * COPIES];
   const int tid = threadIdx.x;
+  const int copy = (tid & 31) % COPIES;
   const int num_tiles = (int)s.counters[sc_tiles];
   const int per = (int)div_up(num_tiles, gridDim.x);
   const int t0 = blockIdx.x * per, t1 = min(num_tiles, t0 + per);
@@ -479,17 +485,27 @@ seg_histogram(const K* keys, const int64_t* offsets, seg_state_t s) {
   auto flush = [&] {
     __syncthreads();
     if(cur >= 0) {
-      uint32_t* g = s.seg_hist + (int64_t)cur * PASSES * radix_bins;
-      for(int i = tid; i < PASSES * radix_bins; i += NT) {
-        if(sh[i]) atomicAdd(&g[i], sh[i]);
-        sh[i] = 0;
+      uint32_t* g = s.seg_hist + (int64_t)cur * BINS;
+      for(int i = tid; i < BINS; i += NT) {
+        uint32_t sum = 0;
+#pragma unroll
+        for(int j = 0; j < COPIES; ++j) {
+          const int c = (i + j) & (COPIES - 1);
+          sum += sh[i * COPIES + c];
+          sh[i * COPIES + c] = 0;
+        }
+        if(sum) atomicAdd(&g[i], sum);
       }
     } else {
-      for(int i = tid; i < PASSES * radix_bins; i += NT) sh[i] = 0;
+      for(int i = tid; i < BINS * COPIES; i += NT) sh[i] = 0;
     }
     __syncthreads();
   };
   flush();
+  // Loads of a tile are issued UNROLL at a time before their keys are
+  // counted, so each thread has several in flight (one at a time left the
+  // kernel waiting on memory latency).
+  constexpr int UNROLL = 8;
   for(int t = t0; t < t1; ++t) {
     const int l = s.tile_owner[t];
     if(l != cur) { flush(); cur = l; }
@@ -497,11 +513,19 @@ seg_histogram(const K* keys, const int64_t* offsets, seg_state_t s) {
     const int64_t sb = offsets[seg], se = offsets[seg + 1];
     const int64_t b = sb + (int64_t)(t - s.large_tile_base[l]) * TILE;
     const int n = (int)min((int64_t)TILE, se - b);
-    for(int i = tid; i < n; i += NT) {
-      U u = radix_key<K>::to_bits(keys[b + i]);
+    for(int i0 = tid; i0 < n; i0 += NT * UNROLL) {
+      U u[UNROLL];
 #pragma unroll
-      for(int p = 0; p < PASSES; ++p)
-        atomicAdd(&sh[p * radix_bins + extract_digit(u, 8 * p, 8)], 1u);
+      for(int k = 0; k < UNROLL; ++k)
+        if(i0 + k * NT < n) u[k] = radix_key<K>::to_bits(keys[b + i0 + k * NT]);
+#pragma unroll
+      for(int k = 0; k < UNROLL; ++k) {
+        if(i0 + k * NT < n) {
+#pragma unroll
+          for(int p = 0; p < PASSES; ++p)
+            atomicAdd(&sh[(p * radix_bins + extract_digit(u[k], 8 * p, 8)) * COPIES + copy], 1u);
+        }
+      }
     }
   }
   flush();
