@@ -39,7 +39,7 @@ SEED = 0x6D677075 + 2
 METRIC = "Mkeys/s (2^28 u32 key + u32 value radix sort)"
 ALG_BYTES_PER_KEY = 68          # 4 passes x (4+4 read + 4+4 write) + 4 histogram read
 PASS_BYTES_PER_KEY = 16         # one onesweep_pass launch
-ONESWEEP_TRAFFIC_PER_KEY = 14.7  # measured DRAM bytes per key of one pass
+ONESWEEP_TRAFFIC_PER_KEY = 14.62  # measured DRAM bytes per key of one pass
 CPU_SAMPLE = 1 << 24
 
 

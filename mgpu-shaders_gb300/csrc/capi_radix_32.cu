@@ -32,14 +32,17 @@ mgpu_status_t radix_sort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys,
       typedef std::remove_pointer_t<decltype(vp)> V;
       K* k = (K*)keys;
       V* v = (V*)vals;
+      // Odd item counts: a half-warp's run starts 16 banks from its
+      // neighbour's.
+      constexpr int V0 = radix_tuning<4>::vt, V1 = 31, V2 = 23;
       if(d_count)   // count read on the device: the default shape
-        return sort_shape<384, 20, 3, true>(c, k, v, count, aux, aux_size, d_count);
+        return sort_shape<384, V0, 3, true>(c, k, v, count, aux, aux_size, d_count);
       switch(variant) {
-        case 1: return sort_shape<256, 32, 3>(c, k, v, count, aux, aux_size, nullptr);
-        case 2: return sort_shape<256, 24, 3>(c, k, v, count, aux, aux_size, nullptr);
+        case 1: return sort_shape<256, V1, 3>(c, k, v, count, aux, aux_size, nullptr);
+        case 2: return sort_shape<256, V2, 3>(c, k, v, count, aux, aux_size, nullptr);
         case 3: return sort_shape4<256, 16>(c, k, v, count, aux, aux_size);
         case 4: return sort_shape4<128, 16>(c, k, v, count, aux, aux_size);
-        default: return sort_shape<384, 20, 3>(c, k, v, count, aux, aux_size, nullptr);
+        default: return sort_shape<384, V0, 3>(c, k, v, count, aux, aux_size, nullptr);
       }
     };
     if(val_bytes == 0) return go((no_values*)nullptr);

@@ -8,13 +8,13 @@
 namespace variants {
 
 // radix_sort onesweep tiles: 8-bit digits at 3 CTAs/SM, 4-byte keys
-// {384x20, 256x32, 256x24} (with 8-byte values each holds half the keys per
+// {384x19, 256x31, 256x23} (with 8-byte values each holds half the keys per
 // thread), 8-byte keys {256x16, 256x12, 384x10}; then 4-bit digits (twice
 // the passes, ranking in registers) {256x16/4b, 128x16/4b} for both.  The
 // tuner thus picks the digit width as well as the shape.
 inline int radix_count(int) { return 5; }
 inline const char* radix_name(int key_bytes, int v) {
-  static const char* n4[] = { "384x20", "256x32", "256x24", "256x16/4b", "128x16/4b" };
+  static const char* n4[] = { "384x19", "256x31", "256x23", "256x16/4b", "128x16/4b" };
   static const char* n8[] = { "256x16", "256x12", "384x10", "256x16/4b", "128x16/4b" };
   return key_bytes == 4 ? n4[v] : n8[v];
 }

@@ -42,6 +42,7 @@ namespace device {
 struct no_values {};
 
 constexpr int radix_bins = 256;
+
 constexpr uint32_t lb_agg = 1u << 30;
 constexpr uint32_t lb_inc = 2u << 30;
 constexpr uint32_t lb_count = (1u << 30) - 1;
@@ -72,9 +73,9 @@ struct onesweep_args {
 //   A  the staged tile: keys (raw on the first pass), later the values; 16
 //      spare bytes take the aligned window of a tile that does not start on
 //      16 bytes;
-//   B  the warps' match words while ranking (2 KB per warp), then the keys
+//   B  the match words while ranking (1 KB per half-warp), then the keys
 //      in local digit order, then the values in that order;
-//   W  each warp's digit offsets within the tile;
+//   W  each half-warp's digit offsets within the tile (16-bit);
 //   plus the digits' global bases, scan scratch, the mbarrier and the tile id.
 template<typename K, typename V, int NT, int ITEMS>
 struct onesweep_layout {
@@ -86,7 +87,7 @@ struct onesweep_layout {
   static constexpr size_t a_off = 0;
   static constexpr size_t b_off = a_off + elem * tile + 16;
   static constexpr size_t w_off = b_off + elem * tile;
-  static constexpr size_t w_bytes = (size_t)num_warps * radix_bins * 4;
+  static constexpr size_t w_bytes = (size_t)2 * num_warps * radix_bins * 2;
   static constexpr size_t gbase_off = w_off + w_bytes;
   static constexpr size_t scan_off = gbase_off + sizeof(int) * radix_bins;
   static constexpr size_t bar_off = scan_off + sizeof(uint32_t) * 32;
@@ -95,8 +96,8 @@ struct onesweep_layout {
   static_assert(NT >= radix_bins && NT % 32 == 0, "one thread per digit");
   static_assert((sizeof(U) * tile) % 16 == 0, "bulk-copy granularity");
   static_assert(elem * tile >= (size_t)num_warps * 2 * radix_bins * 4,
-    "the warps' match words fit in region B");
-  static_assert(ITEMS % 2 == 0 && tile <= 65536, "ranks are packed 16-bit pairs");
+    "the half-warps' match words fit in region B");
+  static_assert(tile <= 65536, "ranks are packed 16-bit pairs");
 };
 
 // Exclusive scan of two 256-entry arrays held by threads 0..255 (one digit
@@ -304,7 +305,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
 
   unsigned char* A = smem + L::a_off;
   unsigned char* B = smem + L::b_off;
-  uint32_t* W = (uint32_t*)(smem + L::w_off);
+  uint16_t* W = (uint16_t*)(smem + L::w_off);
   int* gbase = (int*)(smem + L::gbase_off);
   uint32_t* stmp = (uint32_t*)(smem + L::scan_off);
   uint64_t* bar = (uint64_t*)(smem + L::bar_off);
@@ -345,7 +346,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     bulk_load(A, a.keys_in + kstart, kbytes, bar);
   }
 
-  // This warp's match words: one 64-bit word per digit, at the start of B.
+  // This warp's match words (its two half-warps' 256 words each), in B.
   uint32_t* mw = (uint32_t*)B + warp * 2 * radix_bins;
   for(int j = lane; j < 2 * radix_bins / 4; j += 32)
     reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
@@ -362,11 +363,17 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     if(lane == 0) { stmp[16 + warp] = m; stmp[24 + warp] = sum; }
   }
 
-  // Element e of item i in this thread: warp-contiguous rows of 32 lanes,
-  // e = warp_base + 32 * i + lane; it is in range while 32 * i < rem.
-  const int warp_base = warp * 32 * ITEMS;
-  const int rem = valid - warp_base - lane;
-  U* const ak = (U*)A + koff + warp_base + lane;        // this thread's staged keys
+  // Ranking rows are 16 lanes wide: each half-warp (a "virtual warp" vw)
+  // owns the contiguous run of 16 * ITEMS elements, and item i of this thread
+  // is element vw * 16 * ITEMS + 16 * i + (lane & 15).  (An odd ITEMS puts the
+  // two halves' runs 16 banks apart.)  Item i is in range while RS * i < rem.
+  constexpr int RS = 16;
+  constexpr int NVW = 2 * NWARPS;
+  const int vw = 2 * warp + (lane >> 4);
+  const int rl = lane & 15;                              // lane within the row
+  const int thr_base = vw * RS * ITEMS + rl;
+  const int rem = valid - thr_base;
+  U* const ak = (U*)A + koff + thr_base;                 // this thread's staged keys
   if(kfill < TILE) {
     // Plain loads; positions past the tile's end take the largest radix
     // bits, so they rank last (after every real key with digit 255).
@@ -375,10 +382,10 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       const K k = radix_key<K>::from_bits(~(U)0);
       memcpy(&fill, &k, sizeof(U));
     }
-    const U* src = a.keys_in + base + warp_base + lane;
+    const U* src = a.keys_in + base + thr_base;
 #pragma unroll 4
     for(int i = 0; i < ITEMS; ++i)
-      if(warp_base + 32 * i + lane >= kfill) ak[32 * i] = 32 * i < rem ? src[32 * i] : fill;
+      if(thr_base + RS * i >= kfill) ak[RS * i] = RS * i < rem ? src[RS * i] : fill;
   }
   {
     // Only warp 0 polls the barrier; the other warps sleep at the CTA
@@ -403,7 +410,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
   // Radix bits of item i (the staged copy holds raw keys on the first pass).
   auto key_bits = [&](int i) -> U {
-    U u = ak[32 * i];
+    U u = ak[RS * i];
     if(a.first) {
       K key;
       memcpy(&key, &u, sizeof(K));
@@ -412,44 +419,43 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     return u;
   };
 
-  // Warp-level stable ranking: item i of every lane forms one row; lanes
-  // holding equal digits are peers.  Per digit, one 64-bit word: one half
-  // collects the row's peer mask (every lane ORs its lane bit in), the
-  // other is the warp's running count.  A lane reads both halves in one
-  // load; the lowest peer writes back the advanced count with a clear mask.
-  // Three shared-memory operations per key.  Digits with bit 4 set keep their
-  // mask in the upper half, so the masks of any 32 digits spread over all 32
-  // banks.  The rank counts earlier rows and lower lanes of the same row
-  // (element order).  Ranks (< 2^16) are kept as packed pairs.
-  uint32_t rp[ITEMS / 2];
+  // Stable ranking by half-warps: item i of the 16 lanes of a half forms one
+  // row; lanes holding equal digits are peers.  Per (half-warp, digit) one
+  // 32-bit word: the low half collects the row's peer mask (every lane ORs
+  // its bit in), the high half is the half-warp's running count.  A lane reads
+  // both in one load; the lowest peer writes back the advanced count with a
+  // cleared mask.  Three 32-bit shared-memory operations per key (32-lane rows
+  // need a 64-bit mask + count word, whose random accesses cost about 1.6x the
+  // wavefronts: 1.295 -> 1.240 ms per 2^28 pass).  The rank counts earlier
+  // rows and lower lanes of the same row (element order).  Ranks (< 2^16) are
+  // kept as packed pairs.
+  uint32_t rp[(ITEMS + 1) / 2];
   {
-    const uint32_t lt_mask = lanemask_lt();
-    const uint32_t lane_bit = 1u << lane;
+    uint32_t* mv = (uint32_t*)B + vw * radix_bins;
+    const uint32_t lt_mask = (1u << rl) - 1;
+    const uint32_t lane_bit = 1u << rl;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
       const uint32_t d = extract_digit(key_bits(i), a.shift, 8);
-      const uint32_t hi = (d >> 4) & 1;            // mask in the upper half
       uint32_t rank;
-      if(check_uniform && __all_sync(0xffffffffu, d == __shfl_sync(0xffffffffu, d, 0))) {
-        // One digit across the row (common once equal keys sit together):
-        // the peers are the whole warp, and same-address atomics are skipped.
-        uint32_t* cw = &mw[2 * d + 1 - hi];
-        const uint32_t cnt = *cw;
+      if(check_uniform && __all_sync(0xffffffffu, d == __shfl_sync(0xffffffffu, d, lane & 16))) {
+        // One digit across each half-row (common once equal keys sit
+        // together): the peers are the whole half, same-address atomics are
+        // skipped, and its lane 0 advances the count.
+        uint32_t* cw = &mv[d];
+        const uint32_t cnt = *cw >> 16;
         __syncwarp();
-        if(lane == 0) *cw = cnt + 32;
+        if(rl == 0) *cw = (cnt + 16) << 16;
         __syncwarp();
-        rank = cnt + lane;
+        rank = cnt + rl;
       } else {
-        atomicOr(&mw[2 * d + hi], lane_bit);
+        atomicOr(&mv[d], lane_bit);
         __syncwarp();
-        const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
+        const uint32_t w = mv[d];
         __syncwarp();
-        const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
+        const uint32_t peers = w & 0xffffu, cnt = w >> 16;
         const uint32_t below = peers & lt_mask;
-        if(!below) {
-          const uint32_t next = cnt + __popc(peers);
-          *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
-        }
+        if(!below) mv[d] = (cnt + __popc(peers)) << 16;
         __syncwarp();
         rank = cnt + __popc(below);
       }
@@ -459,19 +465,16 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
   __syncthreads();
 
-  // Digit `tid`: counts per warp -> exclusive offsets over warps (kept in
-  // registers); publish the tile's count (inclusive for tile 0) before
-  // scanning, so successors can proceed as early as possible.
+  // Digit `tid`: counts per (virtual) warp -> exclusive offsets over them;
+  // publish the tile's count (inclusive for tile 0) before scanning, so
+  // successors can proceed as early as possible.
+  auto vw_count = [&](int w) -> uint32_t {
+    return ((const uint32_t*)B)[w * radix_bins + tid] >> 16;
+  };
   uint32_t tile_cnt = 0, valid_cnt = 0;
-  uint32_t wexcl[NWARPS];
   if(tid < radix_bins) {
-    const uint32_t hi = (tid >> 4) & 1;
 #pragma unroll
-    for(int w = 0; w < NWARPS; ++w) {
-      const uint32_t c = ((const uint32_t*)B)[w * 2 * radix_bins + 2 * tid + 1 - hi];
-      wexcl[w] = tile_cnt;
-      tile_cnt += c;
-    }
+    for(int w = 0; w < NVW; ++w) tile_cnt += vw_count(w);
     valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
     st_relaxed(&t.lb_row[tid], (tile ? lb_agg : lb_inc) | valid_cnt);
   }
@@ -479,23 +482,30 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   scan_256_pair(tile_start, glob_start, stmp);
 
   // Issue the first look-back window now; its L2 round trip overlaps the
-  // key scatter below.
+  // key scatter below.  Each (virtual) warp's offset of each digit within the
+  // tile goes to W (16-bit entries with 16-lane rows).
   lookback_window_t<WINDOW> lbw;
   if(tid < radix_bins) {
     if(tile > 0) lbw.issue(t.lb_row + tid - radix_bins, tile);
+    uint32_t run = tile_start;
 #pragma unroll
-    for(int w = 0; w < NWARPS; ++w) W[w * radix_bins + tid] = wexcl[w] + tile_start;
+    for(int w = 0; w < NVW; ++w) {
+      const uint32_t c = vw_count(w);
+      W[w * radix_bins + tid] = (uint16_t)run;
+      run += c;
+    }
   }
   __syncthreads();
 
   // Keys into B in local digit order; the ranks become local positions.
   {
-    const uint32_t* wh = W + warp * radix_bins;
+    const uint16_t* wh = W + vw * radix_bins;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
       const U k = key_bits(i);
       const uint32_t sh = (i & 1) * 16;
-      const uint32_t r = ((rp[i >> 1] >> sh) & 0xffffu) + wh[extract_digit(k, a.shift, 8)];
+      const uint32_t dg = extract_digit(k, a.shift, 8);
+      const uint32_t r = ((rp[i >> 1] >> sh) & 0xffffu) + wh[dg];
       rp[i >> 1] = (rp[i >> 1] & ~(0xffffu << sh)) | (r << sh);
       ((U*)B)[r] = k;
     }
@@ -560,7 +570,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     }
   }
   if constexpr(HAS_V) {
-    V* const av = (V*)A + voff + warp_base + lane;     // this thread's staged values
+    V* const av = (V*)A + voff + thr_base;             // this thread's staged values
     // The sorted keys must have left B, and (when copied) the values arrived.
     bool ok = true;
     if(bulk_v && warp == 0) ok = mbar_wait_bounded(bar, vparity, a.error, a.wait_limit);
@@ -569,15 +579,15 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       return;
     }
     if(vfill < valid) {
-      const V* src = a.vals_in + base + warp_base + lane;
+      const V* src = a.vals_in + base + thr_base;
 #pragma unroll 4
       for(int i = 0; i < ITEMS; ++i)
-        if(32 * i < rem && warp_base + 32 * i + lane >= vfill) av[32 * i] = src[32 * i];
+        if(RS * i < rem && thr_base + RS * i >= vfill) av[RS * i] = src[RS * i];
       __syncwarp();                        // each warp reads only its own rows
     }
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i)
-      if(32 * i < rem) ((V*)B)[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = av[32 * i];
+      if(RS * i < rem) ((V*)B)[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = av[RS * i];
     __syncthreads();
     V* vals_out = a.vals_out + t.out_base;
 #pragma unroll

@@ -26,11 +26,14 @@ namespace mgpu {
 namespace gb300 {
 
 // Default onesweep tile shapes (threads, keys per thread, CTAs per SM) by
-// the width of the staged elements (the wider of key and value): 7680-key
-// tiles of 12 warps for 4-byte elements, 4096-key tiles of 8 warps for
-// 8-byte ones; three CTAs of about 73 KB of shared memory per SM either way.
+// the width of the staged elements (the wider of key and value): 7296-key
+// tiles of 12 warps for 4-byte elements (19 keys per thread: an odd count
+// keeps the two half-warps' runs in different banks), 4096-key tiles of 8
+// warps for 8-byte ones (64-bit reads serve each half-warp separately, so
+// any count is conflict-free); three CTAs of about 70 KB of shared memory per
+// SM either way.
 template<int elem_bytes> struct radix_tuning;
-template<> struct radix_tuning<4> { enum { nt = 384, vt = 20, min_blocks = 3 }; };
+template<> struct radix_tuning<4> { enum { nt = 384, vt = 19, min_blocks = 3 }; };
 template<> struct radix_tuning<8> { enum { nt = 256, vt = 16, min_blocks = 3 }; };
 
 template<typename K, typename V>
