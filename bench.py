@@ -1043,6 +1043,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the short runs of the other configurations")
     ap.add_argument("--secondary-steps", type=int, default=10)
+    ap.add_argument("--radix-variant", type=int, default=None,
+                    help="headline sort with this tuning variant (mgpu_tuning_variants order)")
     ap.add_argument("--no-comparator", action="store_true",
                     help="skip the informational CUB radix sort on the headline input")
     ap.add_argument("--seg-count", type=int, default=100_000,
@@ -1069,6 +1071,10 @@ def main():
     n = args.n
     steps, warmup = args.steps, max(3, args.warmup)
     ctx = mg.Context(local)
+    if args.radix_variant is not None:
+        # A compiled launch shape / digit width of the tuner's list instead of
+        # the default (e.g. 3: 4-bit digits); for shape studies and captures.
+        ctx.tuning_set("radix", np.uint32, 4, -1, args.radix_variant)
     keys_h, vals_h = make_input(n, dist=args.dist, seed=SEED + rank)
 
     # Each step sorts an unsorted 2 GiB copy (> L2), restored from the pristine
@@ -1163,6 +1169,8 @@ def main():
     nbytes = 4 * n
     streams = [torch.cuda.Stream() for _ in range(3)]          # upload, sort, download
     up, srt, down = [mg.Context(local, stream=st_.cuda_stream) for st_ in streams]
+    if args.radix_variant is not None:
+        srt.tuning_set("radix", np.uint32, 4, -1, args.radix_variant)
 
     def e2e_run(num_steps):
         torch.cuda.synchronize()
@@ -1210,7 +1218,9 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "Mkeys/s", "n_gpus": world, "steps": steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": config(args.dist),
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": dict(config(args.dist), **({} if args.radix_variant is None else
+                                             {"radix_variant": args.radix_variant})),
         "gpu_launches": launches,
         "hbm_gbs_at_68B_per_key": ALG_BYTES_PER_KEY * n / (ms * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "kernel": "onesweep_pass", "achieved": achieved,

@@ -364,14 +364,23 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   }
 
   // Ranking rows are 16 lanes wide: each half-warp (a "virtual warp" vw)
-  // owns the contiguous run of 16 * ITEMS elements, and item i of this thread
-  // is element vw * 16 * ITEMS + 16 * i + (lane & 15).  (An odd ITEMS puts the
-  // two halves' runs 16 banks apart.)  Item i is in range while RS * i < rem.
+  // owns the contiguous run of 16 * rpv elements, and item i < rpv of this
+  // thread is element vw * 16 * rpv + 16 * i + (lane & 15).  A full tile has
+  // rpv = ITEMS rows per half-warp (an odd ITEMS puts the two halves' runs 16
+  // banks apart); a partial tile of the segmented sort (most large segments
+  // end in one) spreads its elements evenly over all half-warps with fewer
+  // rows, so it costs in proportion to its size (seg_onesweep_pass 2.91 ->
+  // 2.64 ms on 10^5 lognormal segments).  Item i is in range while RS * i <
+  // rem.
   constexpr int RS = 16;
   constexpr int NVW = 2 * NWARPS;
+  // (Only the segmented sort spreads: in a plain sort only the last tile is
+  // partial, and a compile-time row count keeps the loops free of checks.)
+  const int rpv = (!UNALIGNED || valid == TILE) ? ITEMS
+                                : max(1, min(ITEMS, (valid + RS * NVW - 1) / (RS * NVW)));
   const int vw = 2 * warp + (lane >> 4);
   const int rl = lane & 15;                              // lane within the row
-  const int thr_base = vw * RS * ITEMS + rl;
+  const int thr_base = vw * RS * rpv + rl;
   const int rem = valid - thr_base;
   U* const ak = (U*)A + koff + thr_base;                 // this thread's staged keys
   if(kfill < TILE) {
@@ -385,7 +394,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     const U* src = a.keys_in + base + thr_base;
 #pragma unroll 4
     for(int i = 0; i < ITEMS; ++i)
-      if(thr_base + RS * i >= kfill) ak[RS * i] = RS * i < rem ? src[RS * i] : fill;
+      if(i < rpv && thr_base + RS * i >= kfill) ak[RS * i] = RS * i < rem ? src[RS * i] : fill;
   }
   {
     // Only warp 0 polls the barrier; the other warps sleep at the CTA
@@ -436,6 +445,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     const uint32_t lane_bit = 1u << rl;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
+      if(i >= rpv) continue;
       const uint32_t d = extract_digit(key_bits(i), a.shift, 8);
       uint32_t rank;
       if(check_uniform && __all_sync(0xffffffffu, d == __shfl_sync(0xffffffffu, d, lane & 16))) {
@@ -475,7 +485,8 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
   if(tid < radix_bins) {
 #pragma unroll
     for(int w = 0; w < NVW; ++w) tile_cnt += vw_count(w);
-    valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(TILE - valid) : 0u);
+    // Padding positions (all-ones bits, digit 255) ranked after the real keys.
+    valid_cnt = tile_cnt - (tid == radix_bins - 1 ? (uint32_t)(RS * NVW * rpv - valid) : 0u);
     st_relaxed(&t.lb_row[tid], (tile ? lb_agg : lb_inc) | valid_cnt);
   }
   uint32_t tile_start = tile_cnt, glob_start = hval;
@@ -502,6 +513,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     const uint16_t* wh = W + vw * radix_bins;
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i) {
+      if(i >= rpv) continue;
       const U k = key_bits(i);
       const uint32_t sh = (i & 1) * 16;
       const uint32_t dg = extract_digit(k, a.shift, 8);
@@ -582,12 +594,12 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
       const V* src = a.vals_in + base + thr_base;
 #pragma unroll 4
       for(int i = 0; i < ITEMS; ++i)
-        if(RS * i < rem && thr_base + RS * i >= vfill) av[RS * i] = src[RS * i];
+        if(i < rpv && RS * i < rem && thr_base + RS * i >= vfill) av[RS * i] = src[RS * i];
       __syncwarp();                        // each warp reads only its own rows
     }
 #pragma unroll
     for(int i = 0; i < ITEMS; ++i)
-      if(RS * i < rem) ((V*)B)[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = av[RS * i];
+      if(i < rpv && RS * i < rem) ((V*)B)[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = av[RS * i];
     __syncthreads();
     V* vals_out = a.vals_out + t.out_base;
 #pragma unroll

@@ -518,19 +518,24 @@ scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_stat
       T acc = op_t::identity();
 #pragma unroll
       for(int r = 0; r < ROWS; ++r) {
-        T v[PER];
+        // In place: the row's items become their running fold, then (after
+        // the warp scan) are offset by the row carry; the exclusive form
+        // shifts by one item from the top down, so no copy of the row is
+        // held (a copy spilled the exclusive kernel at 64 registers).
+        T* yr = y + r * PER;
 #pragma unroll
-        for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], y[r * PER + j]) : y[r * PER];
-        T linc = warp_inclusive_scan(v[PER - 1], op);
+        for(int j = 1; j < PER; ++j) yr[j] = op(yr[j - 1], yr[j]);
+        T linc = warp_inclusive_scan(yr[PER - 1], op);
         T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
         if(lane == 0) lexc = op_t::identity();
         T row_carry = op(acc, lexc);
         if(exclusive) {
 #pragma unroll
-          for(int j = 0; j < PER; ++j) y[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
+          for(int j = PER - 1; j > 0; --j) yr[j] = op(row_carry, yr[j - 1]);
+          yr[0] = row_carry;
         } else {
 #pragma unroll
-          for(int j = 0; j < PER; ++j) y[r * PER + j] = op(row_carry, v[j]);
+          for(int j = 0; j < PER; ++j) yr[j] = op(row_carry, yr[j]);
         }
         acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
       }
