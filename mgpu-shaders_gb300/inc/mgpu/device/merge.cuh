@@ -355,11 +355,12 @@ mergesort_pass_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_o
 // Sorts each tile of NT*VT items: stable odd-even transposition network in
 // registers, then log2(NT) merge passes through shared memory.  With
 // `index_values` the values are synthesised as the global index
-// (mergesort_indices).
+// (mergesort_indices).  `vec`: all four arrays start on 16 bytes, so a full
+// tile moves between global and shared memory as 16-byte vectors.
 template<typename K, typename V, int NT, int VT, bool index_values, typename comp_t>
 __global__ void __launch_bounds__(NT)
 blocksort_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_out, int64_t count,
-  comp_t comp) {
+  comp_t comp, int vec) {
   constexpr bool has_values = !std::is_same<V, no_values>::value;
   constexpr int NV = NT * VT;
   __shared__ __align__(16) K sk[NV + 1];
@@ -370,9 +371,22 @@ blocksort_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_out, i
   const int valid = (int)min((int64_t)NV, count - base);
 
   // Load the tile (coalesced), then take VT consecutive items per thread.
-  for(int i = tid; i < valid; i += NT) {
-    sk[i] = keys_in[base + i];
-    if constexpr(has_values && !index_values) sv[i] = vals_in[base + i];
+  constexpr int KV16 = (int)(sizeof(K) * NV / 16);
+  constexpr int VV16 = has_values ? (int)(sizeof(V) * NV / 16) : 0;
+  constexpr bool vec_ok = (sizeof(K) * NV) % 16 == 0 && (!has_values || (sizeof(V) * NV) % 16 == 0);
+  const bool full_vec = vec_ok && vec && valid == NV;
+  if(full_vec) {
+    const uint4* gk = (const uint4*)(keys_in + base);
+    for(int i = tid; i < KV16; i += NT) reinterpret_cast<uint4*>(sk)[i] = gk[i];
+    if constexpr(has_values && !index_values) {
+      const uint4* gv = (const uint4*)(vals_in + base);
+      for(int i = tid; i < VV16; i += NT) reinterpret_cast<uint4*>(sv)[i] = gv[i];
+    }
+  } else {
+    for(int i = tid; i < valid; i += NT) {
+      sk[i] = keys_in[base + i];
+      if constexpr(has_values && !index_values) sv[i] = vals_in[base + i];
+    }
   }
   __syncthreads();
   K k[VT];
@@ -443,9 +457,18 @@ blocksort_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_out, i
     if constexpr(has_values) sv[VT * tid + i] = v[i];
   }
   __syncthreads();
-  for(int i = tid; i < valid; i += NT) {
-    keys_out[base + i] = sk[i];
-    if constexpr(has_values) vals_out[base + i] = sv[i];
+  if(full_vec) {
+    uint4* gk = (uint4*)(keys_out + base);
+    for(int i = tid; i < KV16; i += NT) gk[i] = reinterpret_cast<const uint4*>(sk)[i];
+    if constexpr(has_values) {
+      uint4* gv = (uint4*)(vals_out + base);
+      for(int i = tid; i < VV16; i += NT) gv[i] = reinterpret_cast<const uint4*>(sv)[i];
+    }
+  } else {
+    for(int i = tid; i < valid; i += NT) {
+      keys_out[base + i] = sk[i];
+      if constexpr(has_values) vals_out[base + i] = sv[i];
+    }
   }
 }
 

@@ -127,9 +127,11 @@ status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys,
   V* v2 = (num_passes && has_values) ? (V*)(base + v_off) : nullptr;
   K* kb = (num_passes & 1) ? k2 : keys;
   V* vb = (num_passes & 1) ? v2 : vals;
+  const int vec = aligned16_host(keys) && aligned16_host(kb) &&
+    (!has_values || (aligned16_host(vals) && aligned16_host(vb)));
   st = ctx.launch("blocksort", [&] {
     blocksort_kernel<K, V, NT, VT, sort_indices, comp_t><<<(unsigned)num_tiles, NT, 0,
-      ctx.stream>>>(keys, vals, kb, vb, count, comp);
+      ctx.stream>>>(keys, vals, kb, vb, count, comp, vec);
   });
   if(st || !num_passes) return st;
 
