@@ -309,7 +309,8 @@ typedef struct mgpu_request_t {
 typedef struct mgpu_server_stats_t {
   int64_t submitted, completed, failed;
   int64_t elements;        /* sum of request element counts completed */
-  double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> completion */
+  double p50_ms, p99_ms, mean_ms, max_ms;   /* submit -> completion, over the most
+                                               recent 2^20 completions */
   size_t peak_bytes;       /* largest admitted footprint total */
   int64_t coalesced;       /* requests that ran in coalesced batches */
   int64_t batches;         /* coalesced batches launched */

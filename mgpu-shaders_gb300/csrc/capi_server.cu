@@ -114,7 +114,11 @@ struct mgpu_server {
   std::thread scheduler;
 
   int64_t submitted = 0, completed = 0, failed = 0, elements = 0;
+  // Latencies of the most recent completions (a ring of latency_window
+  // samples), so a long-running server's record stays bounded.
+  static constexpr size_t latency_window = size_t(1) << 20;
   std::vector<double> latencies;
+  size_t latency_next = 0;
 
   // Device bytes a request needs: its inputs, outputs and the primitive's aux.
   mgpu_status_t footprint(const mgpu_request_t& r, size_t& bytes, size_t& aux) {
@@ -368,8 +372,11 @@ struct mgpu_server {
     if(st == MGPU_OK) {
       ++completed;
       elements += rec->req.count + (rec->req.op == MGPU_REQ_MERGE ? rec->req.count_b : 0);
-      latencies.push_back(std::chrono::duration<double, std::milli>(rec->finish - rec->submit)
-        .count());
+      const double ms = std::chrono::duration<double, std::milli>(rec->finish - rec->submit)
+        .count();
+      if(latencies.size() < latency_window) latencies.push_back(ms);
+      else latencies[latency_next] = ms;
+      latency_next = (latency_next + 1) % latency_window;
     } else {
       ++failed;
     }
@@ -603,16 +610,20 @@ mgpu_status_t mgpu_server_drain(mgpu_server_t* s) {
 
 mgpu_status_t mgpu_server_stats(mgpu_server_t* s, mgpu_server_stats_t* out) {
   if(!s || !out) return MGPU_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(s->mu);
-  *out = {};
-  out->submitted = s->submitted;
-  out->completed = s->completed;
-  out->failed = s->failed;
-  out->elements = s->elements;
-  out->peak_bytes = s->peak;
-  out->coalesced = s->coalesced;
-  out->batches = s->batch_launches;
-  std::vector<double> l = s->latencies;
+  std::vector<double> l;
+  {
+    // Copy under the lock; sort outside it, so the scheduler is not held up.
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = {};
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->elements = s->elements;
+    out->peak_bytes = s->peak;
+    out->coalesced = s->coalesced;
+    out->batches = s->batch_launches;
+    l = s->latencies;
+  }
   if(!l.empty()) {
     std::sort(l.begin(), l.end());
     auto pct = [&](double q) { return l[std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5))]; };
@@ -630,6 +641,7 @@ mgpu_status_t mgpu_server_reset_stats(mgpu_server_t* s) {
   if(!s) return MGPU_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
   s->latencies.clear();
+  s->latency_next = 0;
   s->completed = s->failed = s->elements = 0;
   s->submitted = 0;
   s->coalesced = s->batch_launches = 0;
