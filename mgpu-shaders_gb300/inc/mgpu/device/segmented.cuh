@@ -102,138 +102,6 @@ __device__ __forceinline__ void warp_rank_sort(K* keys, V* vals, int n) {
   }
 }
 
-// Stable LSD radix sort (8-bit digits) of n <= 32 * W * ITEMS keys held in a
-// shared-memory slice, by a group of W warps.  gtid is the thread's index in
-// the group; mwords has W * 512 words (each warp's 256 64-bit match words);
-// tmp has W words.  Keys are radix bits.  The ceil(n / 32) rows of 32 keys are
-// spread evenly over the warps (warp w ranks rows [w * rpw, (w + 1) * rpw), so
-// a short segment does not wait on one warp's long chain); rows past n are
-// skipped (the last partial row pads with all-ones keys, which rank after
-// every real key and land past n).
-// Ranking as in the onesweep pass: per digit one 64-bit word holds the row's
-// peer mask (each lane ORs its bit in) and the warp's running count; a lane
-// reads both in one load and the lowest peer writes back the advanced count
-// with a cleared mask -- three shared-memory operations per key and no ballot
-// chain, which keeps the kernel off the integer pipe's limit.  Digits with
-// bit 4 set keep the mask in the upper half, so the masks of any 32 digits
-// spread over the 32 banks.  Ranks (< 2^16) are kept as packed pairs.
-template<int W, int ITEMS, typename U, typename V>
-__device__ __forceinline__ void group_radix_sort(U* ks, V* vs, int n, uint32_t* mwords,
-  uint32_t* tmp, int passes, int gtid) {
-  constexpr bool HAS_V = !std::is_same<V, no_values>::value;
-  constexpr int G = 32 * W;
-  constexpr int DPT = G >= radix_bins ? 1 : radix_bins / G;   // digits per thread
-  static_assert(G >= radix_bins ? G % radix_bins == 0 : radix_bins % G == 0, "group size");
-  static_assert(ITEMS % 2 == 0 && 32 * W * ITEMS <= 65536, "ranks are packed 16-bit pairs");
-  const int lane = gtid & 31, gw = gtid >> 5;
-  const int rpw = min(ITEMS, (((n + 31) >> 5) + W - 1) / W);         // rows per warp
-  const int warp_base = gw * 32 * rpw;
-  const int rem = n - warp_base - lane;
-  const int rows = min(rpw, max(0, (n - warp_base + 31) >> 5));      // warp-uniform
-  const uint32_t lt_mask = lanemask_lt();
-  const uint32_t lane_bit = 1u << lane;
-  uint32_t* mw = mwords + gw * 2 * radix_bins;
-  // Word holding the count (after the scan: the offset) of digit d.
-  auto cslot = [](uint32_t d) -> uint32_t { return 2 * d + 1 - ((d >> 4) & 1); };
-  auto gsync = [] { if(W == 1) __syncwarp(); else __syncthreads(); };
-  for(int pass = 0; pass < passes; ++pass) {
-    const int shift = 8 * pass;
-    for(int i = gtid; i < W * 2 * radix_bins / 4; i += G)
-      reinterpret_cast<uint4*>(mwords)[i] = make_uint4(0, 0, 0, 0);
-    U k[ITEMS];
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i)
-      if(i < rows) k[i] = 32 * i < rem ? ks[warp_base + 32 * i + lane] : ~(U)0;
-    gsync();
-    uint32_t rp[ITEMS / 2];
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) {
-      if(i < rows) {
-        const uint32_t d = extract_digit(k[i], shift, 8);
-        const uint32_t hi = (d >> 4) & 1;
-        atomicOr(&mw[2 * d + hi], lane_bit);
-        __syncwarp();
-        const uint2 w = *reinterpret_cast<const uint2*>(&mw[2 * d]);
-        __syncwarp();
-        const uint32_t peers = hi ? w.y : w.x, cnt = hi ? w.x : w.y;
-        const uint32_t below = peers & lt_mask;
-        if(!below) {
-          const uint32_t next = cnt + __popc(peers);
-          *reinterpret_cast<uint2*>(&mw[2 * d]) = hi ? make_uint2(next, 0) : make_uint2(0, next);
-        }
-        __syncwarp();
-        const uint32_t rank = cnt + __popc(below);
-        if(i & 1) rp[i >> 1] |= rank << 16;
-        else rp[i >> 1] = rank;
-      }
-    }
-    gsync();
-    // Per digit: the warps' counts -> exclusive offsets over warps, in place.
-    uint32_t tot[DPT];
-    uint32_t sum = 0;
-#pragma unroll
-    for(int j = 0; j < DPT; ++j) {
-      const int d = gtid * DPT + j;
-      uint32_t t = 0;
-      if(d < radix_bins) {
-        const uint32_t c0 = cslot(d);
-        for(int w = 0; w < W; ++w) {
-          const uint32_t c = mwords[w * 2 * radix_bins + c0];
-          mwords[w * 2 * radix_bins + c0] = t;
-          t += c;
-        }
-      }
-      tot[j] = t;
-      sum += t;
-    }
-    // Exclusive scan of `sum` over the group's threads.
-    uint32_t inc = sum;
-#pragma unroll
-    for(int off = 1; off < 32; off <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
-      if(lane >= off) inc += y;
-    }
-    uint32_t excl = inc - sum;
-    if(W > 1) {
-      if(lane == 31) tmp[gw] = inc;
-      gsync();
-      for(int w = 0; w < gw; ++w) excl += tmp[w];
-    }
-#pragma unroll
-    for(int j = 0; j < DPT; ++j) {
-      const int d = gtid * DPT + j;
-      if(d < radix_bins) {
-        const uint32_t c0 = cslot(d);
-        for(int w = 0; w < W; ++w) mwords[w * 2 * radix_bins + c0] += excl;
-      }
-      excl += tot[j];
-    }
-    gsync();
-    // Keys first; values are read from their old places only after that
-    // (fewer live registers), then scattered after a barrier.
-#pragma unroll
-    for(int i = 0; i < ITEMS; ++i) {
-      if(i < rows) {
-        const uint32_t sh = (i & 1) * 16;
-        const uint32_t r = ((rp[i >> 1] >> sh) & 0xffffu) + mw[cslot(extract_digit(k[i], shift, 8))];
-        rp[i >> 1] = (rp[i >> 1] & ~(0xffffu << sh)) | (r << sh);
-        ks[r] = k[i];
-      }
-    }
-    if constexpr(HAS_V) {
-      V v[ITEMS];
-#pragma unroll
-      for(int i = 0; i < ITEMS; ++i)
-        if(i < rows) v[i] = 32 * i < rem ? vs[warp_base + 32 * i + lane] : V();
-      gsync();
-#pragma unroll
-      for(int i = 0; i < ITEMS; ++i)
-        if(i < rows) vs[(rp[i >> 1] >> ((i & 1) * 16)) & 0xffffu] = v[i];
-    }
-    gsync();
-  }
-}
-
 // Stable merge sort of n <= 32 * W * VT keys (radix bits) and values held in
 // shared memory, by a group of W warps (gtid: the thread's index in the
 // group).  Each thread sorts VT consecutive items in registers by odd-even
@@ -315,9 +183,8 @@ __device__ __forceinline__ void group_merge_sort(U* sk, V* sv, int n, int gtid) 
 }
 
 // Shared memory of the in-CTA sorts: the tile's keys (radix bits) and values,
-// then (radix sort only, MWORDS) each warp's 256 64-bit match words, scan
-// scratch and a work-item slot.
-template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, bool MWORDS = true>
+// scan scratch and a work-item slot.
+template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS>
 struct seg_small_layout {
   typedef typename radix_key<K>::bits_t U;
   static constexpr bool has_values = !std::is_same<V, no_values>::value;
@@ -326,38 +193,11 @@ struct seg_small_layout {
   static constexpr int warps = NT / 32;
   static constexpr size_t keys_off = 0;
   static constexpr size_t vals_off = sizeof(U) * tile;
-  static constexpr size_t hist_off = vals_off + (has_values ? sizeof(V) * tile : 0);
-  static constexpr size_t tmp_off = hist_off + (MWORDS ? sizeof(uint32_t) * warps * 2 * radix_bins : 0);
+  static constexpr size_t tmp_off = vals_off + (has_values ? sizeof(V) * tile : 0);
   static constexpr size_t misc_off = tmp_off + sizeof(uint32_t) * 32;
   static constexpr size_t bytes = misc_off + 16;
   static_assert(warps * slice <= tile, "warp slices fit in the tile buffers");
 };
-
-// Whole sort of at most one tile of keys in one CTA (the single-CTA branch
-// of vk::radix_sort, vk/radix.hxx:221-282, with all bits of the key).
-template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES>
-__global__ void __launch_bounds__(NT)
-radix_sort_cta(K* keys, V* vals, int n) {
-  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
-  typedef typename L::U U;
-  constexpr bool HAS_V = L::has_values;
-  extern __shared__ __align__(16) unsigned char smem[];
-  U* ks = (U*)(smem + L::keys_off);
-  V* vs = (V*)(smem + L::vals_off);
-  uint32_t* hist = (uint32_t*)(smem + L::hist_off);
-  uint32_t* tmp = (uint32_t*)(smem + L::tmp_off);
-  const int tid = threadIdx.x;
-  for(int i = tid; i < n; i += NT) {
-    ks[i] = radix_key<K>::to_bits(keys[i]);
-    if constexpr(HAS_V) vs[i] = vals[i];
-  }
-  __syncthreads();
-  group_radix_sort<NT / 32, ITEMS>(ks, vs, n, hist, tmp, PASSES, tid);
-  for(int i = tid; i < n; i += NT) {
-    keys[i] = radix_key<K>::from_bits(ks[i]);
-    if constexpr(HAS_V) vals[i] = vs[i];
-  }
-}
 
 // Copies the n keys (as radix bits) and values of one segment into shared
 // memory, STRIDE threads, t = this thread's index.  Asynchronous element
@@ -385,12 +225,36 @@ __device__ __forceinline__ void seg_stage_in(const K* keys, const V* vals, int n
   }
 }
 
+// Whole sort of at most one tile of keys in one CTA (the single-CTA branch
+// of vk::radix_sort, vk/radix.hxx:221-282, with all bits of the key): a
+// stable merge sort by radix bits in shared memory, whose result is the LSD
+// radix sort's (for one CTA it takes about a quarter of the latency of four
+// in-shared-memory radix passes).
+template<typename K, typename V, int NT, int ITEMS>
+__global__ void __launch_bounds__(NT)
+radix_sort_cta(K* keys, V* vals, int n) {
+  typedef seg_small_layout<K, V, NT, ITEMS, ITEMS> L;
+  typedef typename L::U U;
+  constexpr bool HAS_V = L::has_values;
+  extern __shared__ __align__(16) unsigned char smem[];
+  U* ks = (U*)(smem + L::keys_off);
+  V* vs = (V*)(smem + L::vals_off);
+  const int tid = threadIdx.x;
+  seg_stage_in<NT>(keys, vals, n, ks, vs, tid);
+  __syncthreads();
+  group_merge_sort<NT / 32, ITEMS>(ks, vs, n, tid);
+  for(int i = tid; i < n; i += NT) {
+    keys[i] = radix_key<K>::from_bits(ks[i]);
+    if constexpr(HAS_V) vals[i] = vs[i];
+  }
+}
+
 // Persistent sort of every segment up to one tile: CTA-class segments first
 // (whole CTA), then slice-class and warp-class segments (one warp each).
 template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS, int PASSES, int MINB = 1>
 __global__ void __launch_bounds__(NT, MINB)
 seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
-  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS, false> L;
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> L;
   typedef typename L::U U;
   constexpr bool HAS_V = L::has_values;
   extern __shared__ __align__(16) unsigned char smem[];

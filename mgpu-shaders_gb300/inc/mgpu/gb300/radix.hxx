@@ -42,12 +42,13 @@ constexpr int radix_elem_bytes() {
                                                                                : (int)sizeof(K);
 }
 
-// Shape of the one-CTA sort that takes arrays of at most one such tile (and
-// the segmented sort's segments of at most one tile): it holds the whole tile
-// in registers, so it keeps the smaller tile.
+// Shape of the one-CTA sort that takes arrays of at most one such tile: a
+// merge sort in shared memory with an odd number of keys per thread (so the
+// threads' runs start in distinct banks), as the segmented sort's small
+// segments.
 template<int key_bytes> struct cta_sort_tuning;
-template<> struct cta_sort_tuning<4> { enum { nt = 256, vt = 20 }; };
-template<> struct cta_sort_tuning<8> { enum { nt = 256, vt = 12 }; };
+template<> struct cta_sort_tuning<4> { enum { nt = 256, vt = 21 }; };
+template<> struct cta_sort_tuning<8> { enum { nt = 256, vt = 13 }; };
 
 // Largest count the 30-bit look-back status word can carry.
 constexpr int64_t radix_max_count = (int64_t(1) << 30) - 1;
@@ -88,7 +89,7 @@ status_t radix_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys
     if(count <= 1) return MGPU_OK;
     if(!keys || (has_values && !vals)) return MGPU_ERR_INVALID_ARG;
     typedef seg_small_layout<K, V, cnt, cvt, cvt> SL;
-    auto k1 = radix_sort_cta<K, V, cnt, cvt, cvt, passes>;
+    auto k1 = radix_sort_cta<K, V, cnt, cvt>;
     if(!ctx.allow_smem(k1, SL::bytes)) return MGPU_ERR_CUDA;
     return ctx.launch("radix_sort_cta", [&] {
       k1<<<1, cnt, SL::bytes, ctx.stream>>>(keys, vals, (int)count);

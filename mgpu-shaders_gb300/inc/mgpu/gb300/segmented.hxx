@@ -50,7 +50,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   constexpr int SLICE = 32 * SLICE_ITEMS;
   constexpr int PASSES = sizeof(K);
   constexpr bool has_values = !std::is_same<V, no_values>::value;
-  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS, false> SL;
+  typedef seg_small_layout<K, V, NT, ITEMS, SLICE_ITEMS> SL;
   typedef onesweep_layout<K, V, ONT, OITEMS> OL;
   if(count < 0 || num_segments < 0 || count > radix_max_count || num_segments > INT32_MAX)
     return MGPU_ERR_INVALID_ARG;
