@@ -44,11 +44,12 @@ constexpr int radix_elem_bytes() {
 
 // Shape of the one-CTA sort that takes arrays of at most one such tile: a
 // merge sort in shared memory with an odd number of keys per thread (so the
-// threads' runs start in distinct banks), as the segmented sort's small
-// segments.
+// threads' runs start in distinct banks).  A lone small sort is bound by its
+// latency chain, so the CTA is wide and each thread's run short (1024 x 5:
+// ten merge passes of five serial steps each).
 template<int key_bytes> struct cta_sort_tuning;
-template<> struct cta_sort_tuning<4> { enum { nt = 256, vt = 21 }; };
-template<> struct cta_sort_tuning<8> { enum { nt = 256, vt = 13 }; };
+template<> struct cta_sort_tuning<4> { enum { nt = 1024, vt = 5 }; };
+template<> struct cta_sort_tuning<8> { enum { nt = 1024, vt = 3 }; };
 
 // Largest count the 30-bit look-back status word can carry.
 constexpr int64_t radix_max_count = (int64_t(1) << 30) - 1;
