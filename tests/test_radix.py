@@ -12,7 +12,10 @@ from datagen import wide_keys
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [0, 1, 2, 31, 32, 33, 255, 4095, 4096, 4097, 3 * 4096 + 5, 65536 + 7, 300_001]
+# Around the one-CTA limits (3072 keys of 8 bytes, 5120 of 4 bytes) and the
+# onesweep tiles (4096 for 8-byte keys or values, 7296 otherwise).
+SIZES = [0, 1, 2, 31, 32, 33, 255, 3072, 3073, 4095, 4096, 4097, 5120, 5121, 7296, 7297,
+         3 * 4096 + 5, 2 * 7296 + 1, 65536 + 7, 300_001]
 KEY_TYPES = [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64]
 
 

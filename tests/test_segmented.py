@@ -30,8 +30,12 @@ def bits(a):
     return a.view(np.uint32 if a.dtype.itemsize == 4 else np.uint64)
 
 
+# Class limits: 32 (warp), 32 x 21 = 672 and 32 x 13 = 416 (one warp's
+# slice for 4- and 8-byte elements), 256 x 21 = 5376 and 256 x 13 = 3328 (one
+# CTA); above them onesweep tiles of 7296 (4096) keys, ragged at the end.
 @pytest.mark.parametrize("lens", [
-    [0], [1], [2], [32], [33], [512], [513], [4096], [4097], [0, 5, 0, 70, 1, 0],
+    [0], [1], [2], [32], [33], [416], [417], [512], [513], [672], [673], [3328], [3329],
+    [4096], [4097], [5376], [5377], [7297], [2 * 7296 + 5], [0, 5, 0, 70, 1, 0],
     [10_000, 1, 3, 4096, 4097, 100_000, 31, 512, 600],
 ])
 @pytest.mark.parametrize("kt", [np.uint32, np.float64])
