@@ -277,13 +277,16 @@ MGPU_API mgpu_status_t mgpu_cache_reserve(mgpu_context_t* ctx, size_t bytes);
  * admitted requests copy their host inputs into device buffers drawn from a
  * stream-ordered pool that stays resident, run the primitive on the slot's
  * stream, copy the results back and release their memory, so requests that
- * arrive while others run overlap with them.  Small sorts and integer scans
- * (at most 2^16 elements) queued together with others of the same kind (op,
- * key type, value width, scan type and operator) are coalesced: up to 512 of
- * them (2^22 elements) run as one segmented sort or scan over a packed
- * buffer, one launch sequence for the batch; each result is byte-identical to
- * the one the request gets alone.  Host buffers must stay valid until the
- * request completes (pinned memory gives asynchronous copies). */
+ * arrive while others run overlap with them.  Small sorts, merges of
+ * integer keys by MGPU_LESS and integer scans (at most 2^16 elements) queued
+ * together with others of the same kind (sorts and those merges by key type
+ * and value width; scans by key type, scan type and operator) are coalesced:
+ * up to 512 of them (2^22 elements) run as one segmented sort or scan over a
+ * packed buffer, one launch sequence for the batch (a merge is a segment
+ * holding A then B, whose stable sort is the A-first merge of sorted inputs);
+ * each result is byte-identical to the one the request gets alone.  Host
+ * buffers must stay valid until the request completes (pinned memory gives
+ * asynchronous copies). */
 typedef enum mgpu_request_op_t {
   MGPU_REQ_SORT = 0,   /* radix sort of keys (+ values), in place on device */
   MGPU_REQ_MERGE = 1,  /* merge of sorted A and B (+ values) */

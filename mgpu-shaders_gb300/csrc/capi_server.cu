@@ -10,16 +10,18 @@
 // stream-ordered memory pool whose release threshold is the budget, so memory
 // stays resident between requests instead of returning to the driver.
 //
-// Coalescing: a small sort or scan (at most coalesce_max elements) at the
-// head of the queue is run together with the other queued small requests of
-// the same kind (same op, key type, value width, scan type and operator; up to
-// max_batch requests and batch_elems elements) as ONE segmented sort or
-// segmented scan over a packed device buffer, one request per segment: one
-// fixed launch sequence for the whole batch instead of a launch chain per
-// request.  Each request's result is the same as alone: a segment is sorted
-// in the radix order of mgpu_radix_sort and integer scans are exact, so every
-// result is byte-identical to the request run alone.  Floating-point scans,
-// larger requests and merges run alone.
+// Coalescing: a small sort, integer merge (by less) or integer scan (at most
+// coalesce_max elements) at the head of the queue is run together with the
+// other queued small requests of the same kind (sorts and such merges of the
+// same key type and value width together; scans of the same key type, scan
+// type and operator; up to max_batch requests and batch_elems elements) as ONE
+// segmented sort or segmented scan over a packed device buffer, one request
+// per segment: one fixed launch sequence for the whole batch instead of a
+// launch chain per request.  Every result is byte-identical to the request run
+// alone: a segment is sorted in the radix order of mgpu_radix_sort (a merge's
+// segment holds A then B, and for integer keys the stable sort of that is the
+// A-first stable merge), and integer scans are exact.  Floating-point scans
+// and merges, merges by greater, and larger requests run alone.
 #include "capi.hxx"
 
 #include <algorithm>
@@ -61,18 +63,34 @@ constexpr int64_t coalesce_max = int64_t(1) << 16;
 constexpr int max_batch = 512;
 constexpr int64_t batch_elems = int64_t(1) << 22;
 
-// Floating-point scans stay alone: a segmented scan adds in another order
-// than the plain scan, so their bits would depend on what they ran with.
+bool integer_key(mgpu_dtype_t t) { return t != MGPU_F32 && t != MGPU_F64; }
+
+// Elements a request puts into a batch (a merge: both inputs).
+int64_t batch_count(const mgpu_request_t& r) {
+  return r.count + (r.op == MGPU_REQ_MERGE ? r.count_b : 0);
+}
+
+// A small merge of integer keys by `less` runs as a segment of the batch's
+// segmented sort: A followed by B, stably sorted, is the A-first stable merge
+// (float keys stay alone: the sort orders -0.0 before +0.0, operator< does
+// not).  Floating-point scans stay alone too: a segmented scan adds in
+// another order than the plain scan, so their bits would depend on what they
+// ran with.
+bool sortlike(const mgpu_request_t& r) {
+  return r.op == MGPU_REQ_SORT ||
+    (r.op == MGPU_REQ_MERGE && integer_key(r.key_type) && r.op_arg == MGPU_LESS);
+}
+
 bool coalescible(const mgpu_request_t& r) {
-  const bool float_scan = r.op == MGPU_REQ_SCAN &&
-    (r.key_type == MGPU_F32 || r.key_type == MGPU_F64);
-  return (r.op == MGPU_REQ_SORT || r.op == MGPU_REQ_SCAN) && !float_scan && r.count > 0 &&
-         r.count <= coalesce_max;
+  const bool int_scan = r.op == MGPU_REQ_SCAN && integer_key(r.key_type);
+  const int64_t n = batch_count(r);
+  return (sortlike(r) || int_scan) && n > 0 && n <= coalesce_max;
 }
 
 bool same_kind(const mgpu_request_t& a, const mgpu_request_t& b) {
-  return a.op == b.op && a.key_type == b.key_type && a.val_bytes == b.val_bytes &&
-         (a.op != MGPU_REQ_SCAN || (a.scan_type == b.scan_type && a.op_arg == b.op_arg));
+  if(a.key_type != b.key_type || a.val_bytes != b.val_bytes) return false;
+  if(sortlike(a) || sortlike(b)) return sortlike(a) && sortlike(b);
+  return a.op == b.op && a.scan_type == b.scan_type && a.op_arg == b.op_arg;
 }
 
 // Requests run together as one segmented sort or scan.
@@ -252,7 +270,7 @@ struct mgpu_server {
     const int64_t n = (int64_t)b->recs.size();
     size_t aux = 0;
     mgpu_status_t st;
-    if(r.op == MGPU_REQ_SORT)
+    if(sortlike(r))
       st = mgpu_segmented_sort(sizing, r.key_type, nullptr, (int)vb, nullptr, b->total, nullptr,
         n, nullptr, &aux);
     else
@@ -285,13 +303,18 @@ struct mgpu_server {
     char* dk = (char*)b->dev[0];
     char* dv = (char*)b->dev[1];
     off[0] = 0;
+    auto h2d = [&](void* d, const void* h, size_t bytes) -> bool {
+      return !bytes || cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    };
     for(int64_t i = 0; i < n; ++i) {
       const mgpu_request_t& r = b->recs[i]->req;
-      off[i + 1] = off[i] + r.count;
-      if(cudaMemcpyAsync(dk + kb * off[i], r.keys, kb * r.count, cudaMemcpyHostToDevice, s) !=
-           cudaSuccess ||
-         (vb && cudaMemcpyAsync(dv + vb * off[i], r.vals, vb * r.count, cudaMemcpyHostToDevice,
-           s) != cudaSuccess))
+      off[i + 1] = off[i] + batch_count(r);
+      if(!h2d(dk + kb * off[i], r.keys, kb * r.count) ||
+         (vb && !h2d(dv + vb * off[i], r.vals, vb * r.count)))
+        return MGPU_ERR_CUDA;
+      if(r.op == MGPU_REQ_MERGE &&      // B right after A in the same segment
+         (!h2d(dk + kb * (off[i] + r.count), r.keys_b, kb * r.count_b) ||
+          (vb && !h2d(dv + vb * (off[i] + r.count), r.vals_b, vb * r.count_b))))
         return MGPU_ERR_CUDA;
     }
     if(cudaMemcpyAsync(b->dev[2], off, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s) !=
@@ -299,7 +322,7 @@ struct mgpu_server {
       return MGPU_ERR_CUDA;
     size_t aux = b->aux_bytes;
     mgpu_status_t st;
-    if(r0.op == MGPU_REQ_SORT)
+    if(sortlike(r0))
       st = mgpu_segmented_sort(c, r0.key_type, dk, (int)vb, vb ? dv : nullptr, b->total,
         (const int64_t*)b->dev[2], n, b->dev[3], &aux);
     else
@@ -309,9 +332,10 @@ struct mgpu_server {
     if(st) return st;
     for(int64_t i = 0; i < n; ++i) {
       const mgpu_request_t& r = b->recs[i]->req;
-      if(cudaMemcpyAsync(r.out_keys, dk + kb * off[i], kb * r.count, cudaMemcpyDeviceToHost, s) !=
+      const int64_t m = batch_count(r);
+      if(cudaMemcpyAsync(r.out_keys, dk + kb * off[i], kb * m, cudaMemcpyDeviceToHost, s) !=
            cudaSuccess ||
-         (vb && cudaMemcpyAsync(r.out_vals, dv + vb * off[i], vb * r.count,
+         (vb && cudaMemcpyAsync(r.out_vals, dv + vb * off[i], vb * m,
            cudaMemcpyDeviceToHost, s) != cudaSuccess))
         return MGPU_ERR_CUDA;
     }
@@ -356,9 +380,9 @@ struct mgpu_server {
     for(uint64_t id : queue) {
       request_record* rec = records[id];
       if(!coalescible(rec->req) || !same_kind(rec->req, head->req)) continue;
-      if((int)b->recs.size() == max_batch || b->total + rec->req.count > batch_elems) break;
+      if((int)b->recs.size() == max_batch || b->total + batch_count(rec->req) > batch_elems) break;
       b->recs.push_back(rec);
-      b->total += rec->req.count;
+      b->total += batch_count(rec->req);
     }
     return b;
   }

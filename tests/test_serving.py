@@ -233,29 +233,39 @@ def test_bench_mix_equals_alone(server_cls, oracle, rng):
 
 
 def small_requests(rng, n_req):
-    """Small sorts (keys only and key-value) and integer scans of a few kinds,
-    interleaved, sizes 1 .. 2^16 (the coalescing limit)."""
+    """Small sorts (keys only and key-value), merges (u32 keys, which coalesce
+    with the u32 sorts, and f32 keys, which run alone) and integer scans of a
+    few kinds, interleaved, sizes 1 .. 2^16 (the coalescing limit)."""
     reqs = []
     for i in range(n_req):
         n = int(2 ** rng.uniform(0, 16))
         if i % 7 == 6:
             n = 1 << 16
-        c = i % 4
+        c = i % 6
         if c == 0:
             reqs.append(("sort", gen_keys(rng, n, np.uint32), np.arange(n, dtype=np.uint32)))
         elif c == 1:
             reqs.append(("sort", gen_keys(rng, n, np.float32), None))
         elif c == 2:
             reqs.append(("scan", rng.integers(0, 1 << 20, n).astype(np.int32), "exc"))
-        else:
+        elif c == 3:
             reqs.append(("scan", rng.integers(0, 1 << 40, n).astype(np.uint64), "inc"))
+        else:
+            kt = np.uint32 if c == 4 else np.float32
+            na = n // 2
+            # Few distinct keys, so A and B share many and the A-first rule shows.
+            a = np.sort(gen_keys(rng, na, kt, "distinct256"))
+            b = np.sort(gen_keys(rng, n - na, kt, "distinct256"))
+            reqs.append(("merge", a, np.arange(na, dtype=np.uint32), b,
+                         np.arange(n - na, dtype=np.uint32) + (1 << 30)))
     return reqs
 
 
 def test_small_requests_coalesce(server_cls, oracle, rng):
     # 200 small requests queued behind one large sort that holds the only
     # slot: the queue fills, and the small ones run in coalesced batches (one
-    # segmented sort or scan per batch) with the same bytes as alone.
+    # segmented sort or scan per batch; u32 merges as sort segments) with the
+    # same bytes as alone.
     reqs = small_requests(rng, 200)
     alone = run_alone(server_cls, reqs)
     srv = server_cls(budget_bytes=1 << 30, num_slots=1)
