@@ -862,6 +862,35 @@ def wl_reduce(args, mg, torch):
                  kernels, cfg, "int32", {"matches_host_sum": ok})
 
 
+def wl_saxpy(args, mg, torch):
+    """vk::transform's example operation at scale: y += a * x over 2^28 f32
+    through the C ABI's transform (the generic grid-stride transform kernel
+    over a device lambda); 12 B/element (read x and y, write y)."""
+    n = args.n if args.n != N_KEYS else 1 << 28
+    rng = np.random.default_rng(SEED + 12)
+    x = rng.standard_normal(n).astype(np.float32)
+    y0 = rng.standard_normal(n).astype(np.float32)
+    a = np.float32(1.618)
+    ctx = mg.Context(0)
+    dx, py, dy = mg.DeviceArray.from_numpy(x), mg.DeviceArray.from_numpy(y0), \
+        mg.DeviceArray(n, np.float32)
+
+    def restore(i):
+        dy.copy_from(py)
+
+    def run(i):
+        ctx.transform_saxpy(float(a), dx, dy)
+
+    steps, warmup = args.steps, max(3, args.warmup)
+    ms, launches, clk = _timed(ctx, run, restore, steps, warmup, 0)
+    ok = bool(np.allclose(dy.numpy(), y0 + a * x, rtol=1e-6, atol=1e-6))
+    roof, kernels = _roofline(ctx, run, restore, 3, {"transform": 12 * n})
+    cfg = {"workload": "transform saxpy f32, y += 1.618 x, %d elements" % n, "count": n,
+           "alg_bytes_per_elem": 12, "l2": "inputs larger than L2; y restored outside the events"}
+    return _line("Melems/s", "Melems/s", n, 12 * n, ms, steps, warmup, launches, clk, roof,
+                 kernels, cfg, "f32", {"matches_host_saxpy": ok})
+
+
 def wl_scan_noalloc(args, mg, torch):
     """2^28 int32 U[0,100) exclusive plus-scan through mgpu_scan_noalloc
     (one tile per CTA, scratch inside the library); 8 B/element."""
@@ -924,6 +953,7 @@ WORKLOADS = {
     "radix_small": wl_radix_small,
     "reduce": wl_reduce,
     "scan_noalloc": wl_scan_noalloc,
+    "saxpy": wl_saxpy,
 }
 
 
