@@ -372,12 +372,16 @@ struct mgpu_server {
   }
 
   // Gathers the queued requests that run together with the queue head (at
-  // least the head itself).  Lock held.
+  // least the head itself), looking at most gather_window entries deep so a
+  // long backlog does not make each admission scan all of it.  Lock held.
+  static constexpr int gather_window = 4 * max_batch;
   batch_record* gather_batch() {
     request_record* head = records[queue.front()];
     batch_record* b = new(std::nothrow) batch_record;
     if(!b) return nullptr;
+    int seen = 0;
     for(uint64_t id : queue) {
+      if(++seen > gather_window) break;
       request_record* rec = records[id];
       if(!coalescible(rec->req) || !same_kind(rec->req, head->req)) continue;
       if((int)b->recs.size() == max_batch || b->total + batch_count(rec->req) > batch_elems) break;
@@ -439,10 +443,14 @@ struct mgpu_server {
             // Admit the batch: its requests leave the queue together.
             b->id = next_batch++;
             for(request_record* r : b->recs) {
-              queue.erase(std::find(queue.begin(), queue.end(), r->id));
               r->slot = slot;
               r->batch = b->id;
             }
+            // One pass over the gathered window removes them all.
+            const auto window_end = queue.begin() +
+              (std::ptrdiff_t)std::min<size_t>(queue.size(), gather_window);
+            queue.erase(std::remove_if(queue.begin(), window_end,
+              [&](uint64_t id) { return records[id]->batch == b->id; }), window_end);
             used += b->footprint;
             peak = std::max(peak, used);
             slot_busy[slot] = 1;
