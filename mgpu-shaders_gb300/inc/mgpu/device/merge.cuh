@@ -83,6 +83,37 @@ __device__ __forceinline__ int64_t merge_path_warp(const K* a, int64_t a_count, 
   return mask ? begin + __ffs(mask) - 1 : end;
 }
 
+// merge_path with either bound (the reference's merge_path<bounds>,
+// common/cta_merge.hxx:10-31): UPPER = false is the lower bound above (A's
+// item first on ties); UPPER = true takes B's item first on ties (predicate
+// comp(a, b)).
+template<bool UPPER, typename K, typename comp_t, typename idx_t>
+__device__ __forceinline__ idx_t merge_path_bounds(const K* a, idx_t a_count, const K* b,
+  idx_t b_count, idx_t diag, comp_t comp) {
+  idx_t begin = diag > b_count ? diag - b_count : 0;
+  idx_t end = diag < a_count ? diag : a_count;
+  while(begin < end) {
+    idx_t mid = (begin + end) >> 1;
+    const K ak = a[mid], bk = b[diag - 1 - mid];
+    const bool pred = UPPER ? comp(ak, bk) : !comp(bk, ak);
+    if(pred) begin = mid + 1;
+    else end = mid;
+  }
+  return begin;
+}
+
+// Partitions at every `spacing` outputs with a chosen bound, one thread each
+// (vk::merge_path_partitions, vk/partition.hxx:9-20); mp_t: the caller's
+// partition type (int in the reference).
+template<bool UPPER, typename K, typename comp_t, typename mp_t>
+__global__ void merge_path_partitions_kernel(const K* a, int64_t a_count, const K* b,
+  int64_t b_count, int64_t spacing, int64_t num_partitions, mp_t* mp, comp_t comp) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= num_partitions) return;
+  const int64_t diag = min(i * spacing, a_count + b_count);
+  mp[i] = (mp_t)merge_path_bounds<UPPER>(a, a_count, b, b_count, diag, comp);
+}
+
 // Partitions of a two-array merge: mp[i] for diagonal min(i * spacing,
 // total).  WARP: one warp per partition (few partitions: the search latency
 // dominates); otherwise one thread per partition (many partitions: the

@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -237,6 +238,55 @@ struct cmd_buffer_t {
   void host_barrier() {}
   void memcpy(void* dest, const void* source, size_t size) { context.memcpy(dest, source, size); }
   context_t& context;
+};
+
+// Drop-in for vk::memcache_t (vk/context.hxx:110-134): a grow-only device
+// scratch buffer of its own (apart from the context's aux cache, which the
+// primitives use).  allocate() returns the buffer's start, grown to at least
+// the size asked for; growing releases the old block in stream order, so
+// work already enqueued on the context's stream that uses it is unaffected,
+// but the pointers an earlier allocate() returned are then stale.  The array
+// form carves 256-byte-aligned pieces of one allocation.
+struct memcache_t {
+  explicit memcache_t(context_t& c) : context(c) {}
+  ~memcache_t() { if(data) cudaFreeAsync(data, context.stream); }
+  memcache_t(const memcache_t&) = delete;
+  memcache_t& operator=(const memcache_t&) = delete;
+
+  template<typename type_t>
+  type_t* allocate(size_t count) { return (type_t*)allocate(sizeof(type_t) * count); }
+
+  void* allocate(size_t size) {
+    if(size > capacity) {
+      if(data) context.check(cudaFreeAsync(data, context.stream));
+      data = nullptr;
+      capacity = 0;
+      if(context.check(cudaMallocAsync(&data, size, context.stream))) return nullptr;
+      capacity = size;
+    }
+    return data;
+  }
+
+  template<size_t count>
+  std::array<void*, count> allocate(std::array<size_t, count> sizes) {
+    std::array<void*, count> out;
+    allocate(sizes.data(), (int)count, out.data());
+    return out;
+  }
+
+  void allocate(const size_t* sizes, int count, void** allocations) {
+    size_t total = 0;
+    for(int i = 0; i < count; ++i) total += (sizes[i] + 255) & ~(size_t)255;
+    char* p = (char*)allocate(total);
+    for(int i = 0; i < count; ++i) {
+      allocations[i] = p;
+      if(p) p += (sizes[i] + 255) & ~(size_t)255;
+    }
+  }
+
+  context_t& context;
+  void* data = nullptr;
+  size_t capacity = 0;
 };
 
 inline bool aligned16_host(const void* p) { return 0 == ((uintptr_t)p & 15); }

@@ -21,6 +21,40 @@ namespace gb300 {
 template<typename T> using less_t = device::less_t<T>;
 template<typename T> using greater_t = device::greater_t<T>;
 
+// Drop-ins for the reference's partition helpers (common/types.hxx:73-76,
+// common/cta_merge.hxx:6-8, vk/partition.hxx:9-20): merge_path_partitions
+// writes mp_data[i] = the merge path of diagonal min(i * spacing, a_count +
+// b_count) for i < num_merge_partitions(a_count + b_count, spacing), with the
+// lower bound (A first on ties) or the upper one (B first).  One thread per
+// partition, enqueued on the context's stream.
+enum bounds_t { bounds_lower, bounds_upper };
+
+constexpr int64_t num_merge_partitions(int64_t count, int64_t spacing) {
+  return (count + spacing - 1) / spacing + 1;
+}
+
+template<bounds_t bounds = bounds_lower, typename K, typename mp_t, typename comp_t>
+status_t merge_path_partitions(context_t& ctx, const K* a, int64_t a_count, const K* b,
+  int64_t b_count, mp_t* mp_data, int64_t spacing, comp_t comp) {
+  if(a_count < 0 || b_count < 0 || spacing < 1 || !mp_data) return MGPU_ERR_INVALID_ARG;
+  if((a_count && !a) || (b_count && !b)) return MGPU_ERR_INVALID_ARG;
+  const int64_t n = num_merge_partitions(a_count + b_count, spacing);
+  return ctx.launch("merge_path_partitions", [&] {
+    device::merge_path_partitions_kernel<bounds == bounds_upper>
+      <<<(unsigned)((n + 255) / 256), 256, 0, ctx.stream>>>(a, a_count, b, b_count, spacing, n,
+        mp_data, comp);
+  });
+}
+
+// Source compatibility with the reference's call shape (cmd_buffer first,
+// partitions before spacing: vk/partition.hxx:11-13).
+template<bounds_t bounds, typename K, typename mp_t, typename comp_t>
+status_t merge_path_partitions(cmd_buffer_t& cmd_buffer, const K* a, int64_t a_count,
+  const K* b, int64_t b_count, mp_t* mp_data, int64_t spacing, comp_t comp) {
+  return merge_path_partitions<bounds>(cmd_buffer.context, a, a_count, b, b_count, mp_data,
+    spacing, comp);
+}
+
 template<int key_bytes> struct merge_tuning;
 // Odd items per thread keep the per-thread strides of the serial merge and of
 // the output staging odd in shared memory, so they do not collide on banks.

@@ -177,5 +177,45 @@ int main() {
     // Histogram + eight 4-bit passes, where the 8-bit shape runs four.
     CHECK(launches == 9, "radix_sort_4bit_passes");
   }
+
+  // merge_path_partitions with both bounds (vk/partition.hxx:9-20) into
+  // buffers from a memcache_t (vk/context.hxx:110-134), against a host merge
+  // path of the same bound.
+  {
+    const int na = 5000, nb = 3000, spacing = 128;
+    std::vector<int> ha(na), hb(nb);
+    srand(11);
+    for(int& x : ha) x = rand() % 1000;
+    for(int& x : hb) x = rand() % 1000;
+    std::sort(ha.begin(), ha.end());
+    std::sort(hb.begin(), hb.end());
+    memcache_t cache(context);
+    auto bufs = cache.allocate<4>({ sizeof(int) * na, sizeof(int) * nb, 0, 0 });
+    const int np = (int)num_merge_partitions(na + nb, spacing);
+    int* mp = (int*)context.alloc_gpu<int>(2 * np);
+    int* da = (int*)bufs[0];
+    int* db = (int*)bufs[1];
+    context.memcpy(da, ha.data(), sizeof(int) * na);
+    context.memcpy(db, hb.data(), sizeof(int) * nb);
+    merge_path_partitions<bounds_lower>(cmd_buffer, da, na, db, nb, mp, spacing, less_t<int>());
+    merge_path_partitions<bounds_upper>(context, da, na, db, nb, mp + np, spacing, less_t<int>());
+    std::vector<int> hmp(2 * np);
+    context.memcpy(hmp.data(), mp, sizeof(int) * 2 * np);
+    if(context.synchronize()) return 2;
+    bool ok = bufs[0] != nullptr && ((uintptr_t)bufs[1] & 255) == 0;
+    for(int u = 0; u < 2; ++u) {
+      for(int i = 0; i < np; ++i) {
+        const int diag = std::min(i * spacing, na + nb);
+        int lo = std::max(0, diag - nb), hi = std::min(diag, na);
+        while(lo < hi) {
+          const int mid = (lo + hi) / 2;
+          const bool pred = u ? ha[mid] < hb[diag - 1 - mid] : !(hb[diag - 1 - mid] < ha[mid]);
+          if(pred) lo = mid + 1; else hi = mid;
+        }
+        ok &= hmp[u * np + i] == lo;
+      }
+    }
+    CHECK(ok, "merge_path_partitions_memcache");
+  }
   return 0;
 }

@@ -31,7 +31,7 @@ def test_cpp_template_api(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     for name in ["launch_transform", "mergesort_user_comparator", "merge_keys",
                  "scan_exclusive_in_place", "radix_sort_keys", "radix_sort_keys_4bit",
-                 "radix_sort_4bit_passes"]:
+                 "radix_sort_4bit_passes", "merge_path_partitions_memcache"]:
         assert "ok " + name in r.stdout
 
 
