@@ -973,11 +973,16 @@ def _summary(line):
         out["inclusive"] = line["inclusive"]
     if "plain_calls" in line:
         out["plain_calls"] = line["plain_calls"]
+    if "loads" in line:                       # the serving loop
+        out["saturation"] = line["saturation"]
+        out["serial_saturation"] = line["serial_saturation"]
+        out["loads"] = line["loads"]
+        out["checks_pass"] = all(ld["server"]["failed"] == 0 for ld in line["loads"])
     return out
 
 
 SECONDARY = ["radix_u64", "radix_f32", "radix_f32_normal", "mergesort", "merge", "scan_i32",
-             "scan_f32", "segsort", "segscan"]
+             "scan_f32", "segsort", "segscan", "serving"]
 
 
 def cub_comparator(torch, keys_h, vals_h, steps, warmup):
@@ -1033,6 +1038,9 @@ def run_secondary(args, mg, torch):
     configuration, summarised for the headline line."""
     sub = argparse.Namespace(**vars(args))
     sub.steps, sub.warmup, sub.n = args.secondary_steps, max(3, args.warmup), N_KEYS
+    # A shorter serving run than its own workload's default (20 repetitions
+    # of the request pool at saturation, 3 s per load level).
+    sub.serve_reps, sub.serve_seconds = min(args.serve_reps, 20), min(args.serve_seconds, 3.0)
     out = {}
     for name in SECONDARY:
         try:
