@@ -519,9 +519,7 @@ scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_stat
 #pragma unroll
       for(int r = 0; r < ROWS; ++r) {
         // In place: the row's items become their running fold, then (after
-        // the warp scan) are offset by the row carry; the exclusive form
-        // shifts by one item from the top down, so no copy of the row is
-        // held (a copy spilled the exclusive kernel at 64 registers).
+        // the warp scan) are offset by the row carry.
         T* yr = y + r * PER;
 #pragma unroll
         for(int j = 1; j < PER; ++j) yr[j] = op(yr[j - 1], yr[j]);
@@ -529,14 +527,8 @@ scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_stat
         T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
         if(lane == 0) lexc = op_t::identity();
         T row_carry = op(acc, lexc);
-        if(exclusive) {
 #pragma unroll
-          for(int j = PER - 1; j > 0; --j) yr[j] = op(row_carry, yr[j - 1]);
-          yr[0] = row_carry;
-        } else {
-#pragma unroll
-          for(int j = 0; j < PER; ++j) yr[j] = op(row_carry, yr[j]);
-        }
+        for(int j = 0; j < PER; ++j) yr[j] = op(row_carry, yr[j]);
         acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
       }
       if(lane == 0) warp_tot[warp] = acc;
@@ -551,6 +543,23 @@ scan_defer_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_stat
       if(tid == 0 && reduction && base + TILE >= count) *reduction = op(prefix, ptot);
 #pragma unroll
       for(int i = 0; i < VT; ++i) y[i] = op(wexc, y[i]);
+      if(exclusive) {
+        // Inclusive -> exclusive: each item takes its predecessor's value,
+        // rows from the last down, so the value a row's lane 0 needs (lane
+        // 31's last item of the row before) is still the inclusive one; the
+        // warp's first item takes the warp's exclusive prefix.  (Shifting
+        // inside the row loop instead kept more values live and spilled.)
+#pragma unroll
+        for(int r = ROWS - 1; r >= 0; --r) {
+          T* yr = y + r * PER;
+          T before = __shfl_up_sync(0xffffffffu, yr[PER - 1], 1);
+          const T row_before = r > 0 ? __shfl_sync(0xffffffffu, y[r * PER - 1], 31) : wexc;
+          if(lane == 0) before = row_before;
+#pragma unroll
+          for(int j = PER - 1; j > 0; --j) yr[j] = yr[j - 1];
+          yr[0] = before;
+        }
+      }
       S::store(out + base, valid, vec, warp, lane, y);
     }
     __syncthreads();
