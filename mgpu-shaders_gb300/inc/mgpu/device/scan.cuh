@@ -341,25 +341,21 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   T x[VT];
   S::load(in + base, valid, vec, warp, lane, x, op_t::identity());
 
-  // Warp-local scan, row by row: within each 16-byte vector, then across the
-  // lanes' vector totals, then the carry of the earlier rows.
+  // Warp-local inclusive scan, row by row, in place: within each 16-byte
+  // vector, then across the lanes' vector totals, then the carry of the
+  // earlier rows.
   T acc = op_t::identity();
 #pragma unroll
   for(int r = 0; r < ROWS; ++r) {
-    T v[PER];
+    T* xr = x + r * PER;
 #pragma unroll
-    for(int j = 0; j < PER; ++j) v[j] = j ? op(v[j - 1], x[r * PER + j]) : x[r * PER];
-    T linc = warp_inclusive_scan(v[PER - 1], op);
+    for(int j = 1; j < PER; ++j) xr[j] = op(xr[j - 1], xr[j]);
+    T linc = warp_inclusive_scan(xr[PER - 1], op);
     T lexc = __shfl_up_sync(0xffffffffu, linc, 1);
     if(lane == 0) lexc = op_t::identity();
-    T row_carry = op(acc, lexc);
-    if(exclusive) {
+    const T row_carry = op(acc, lexc);
 #pragma unroll
-      for(int j = 0; j < PER; ++j) x[r * PER + j] = j ? op(row_carry, v[j - 1]) : row_carry;
-    } else {
-#pragma unroll
-      for(int j = 0; j < PER; ++j) x[r * PER + j] = op(row_carry, v[j]);
-    }
+    for(int j = 0; j < PER; ++j) xr[j] = op(row_carry, xr[j]);
     acc = op(acc, __shfl_sync(0xffffffffu, linc, 31));
   }
   if(lane == 0) warp_tot[warp] = acc;
@@ -385,6 +381,21 @@ scan_kernel(const T* in, T* out, int64_t count, T init, op_t op, tile_status_t<T
   const T carry = warp_tot[warp];
 #pragma unroll
   for(int i = 0; i < VT; ++i) x[i] = op(carry, x[i]);
+  if(exclusive) {
+    // Each item takes its predecessor's inclusive value (rows from the last
+    // down; the warp's first item takes the warp's carry), as in the
+    // deferred scan.
+#pragma unroll
+    for(int r = ROWS - 1; r >= 0; --r) {
+      T* xr = x + r * PER;
+      T before = __shfl_up_sync(0xffffffffu, xr[PER - 1], 1);
+      const T row_before = r > 0 ? __shfl_sync(0xffffffffu, x[r * PER - 1], 31) : carry;
+      if(lane == 0) before = row_before;
+#pragma unroll
+      for(int j = PER - 1; j > 0; --j) xr[j] = xr[j - 1];
+      xr[0] = before;
+    }
+  }
   S::store(out + base, valid, vec, warp, lane, x);
 }
 
