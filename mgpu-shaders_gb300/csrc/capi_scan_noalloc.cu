@@ -10,9 +10,12 @@
 // may allocate its aux cache) or caller-provided aux; this entry point needs
 // neither.
 //
-// Its scratch (tile counter, error word, one 64-bit look-back status word per
-// 4096-element tile) lives in the file-scope array below, sized for at most
-// MGPU_SCAN_NOALLOC_MAX_COUNT elements: 65,538 words = 512 KiB + 16 bytes.
+// It runs the same persistent deferred look-back scan as mgpu_scan (resident
+// CTAs looping over 8192-element tiles), so it scans at the same rate.  Its
+// scratch (tile counter, error word, one 64-bit look-back status word per
+// tile) lives in the file-scope array below, sized for at most
+// MGPU_SCAN_NOALLOC_MAX_COUNT elements: 65,538 words = 512 KiB + 16 bytes
+// (the 32,768 tiles of the largest scan use half of the status words).
 // Every GPU that loads this library holds that array until the process exits.
 // All calls share it, and it keeps the last call's contents: each call clears
 // the tile counter and the status words it will use before its kernel runs.
@@ -32,6 +35,7 @@
 #include "mgpu_gb300.h"
 #include "mgpu/device/scan.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace {
@@ -39,11 +43,15 @@ namespace {
 using namespace mgpu::device;
 
 constexpr int kThreads = 256;
-constexpr int kItems = 16;
+constexpr int kItems = 32;
+constexpr int kMinBlocks = 4;
 constexpr int64_t kTile = (int64_t)kThreads * kItems;
-constexpr int64_t kMaxTiles = MGPU_SCAN_NOALLOC_MAX_COUNT / kTile;
+// The array keeps one status word per 4096 elements; the scan uses one per
+// 8192-element tile.
+constexpr int64_t kMaxTiles = MGPU_SCAN_NOALLOC_MAX_COUNT / 4096;
 constexpr int kMaxDevices = 64;
 static_assert(MGPU_SCAN_NOALLOC_MAX_COUNT % kTile == 0, "whole tiles");
+static_assert(MGPU_SCAN_NOALLOC_MAX_COUNT / kTile <= kMaxTiles, "status words fit");
 
 // Word 0: tile counter (low 32 bits).  Word 1: device error word.
 // Words 2 .. 2 + kMaxTiles: look-back status of each tile.
@@ -51,6 +59,7 @@ static __device__ __align__(256) uint64_t g_noalloc_scan_scratch[2 + kMaxTiles];
 
 std::mutex g_setup_mutex;
 uint64_t* g_scratch_address[kMaxDevices] = {};
+int g_sm_count[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device (set up once).
 cudaError_t scratch_address(int device, uint64_t** out) {
@@ -59,15 +68,41 @@ cudaError_t scratch_address(int device, uint64_t** out) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
     if(e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&g_sm_count[device], cudaDevAttrMultiProcessorCount, device);
+    if(e != cudaSuccess) return e;
     g_scratch_address[device] = (uint64_t*)p;
   }
   *out = g_scratch_address[device];
   return cudaSuccess;
 }
 
+// Resident CTAs of the deferred scan kernel per SM (an occupancy query; no
+// allocation).
+template<typename K>
+int resident_ctas(K kernel, size_t smem) {
+  int n = 0;
+  if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kThreads, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+template<typename T, typename op_t, bool exclusive>
+mgpu_status_t launch_defer(cudaStream_t stream, const T* in, T* out, int64_t count, T init,
+  T* reduction, tile_status_t<T> status, uint32_t* counter, int* error, int vec, int sm_count) {
+  typedef scan_defer_layout<T, kThreads, kItems> L;
+  auto k = scan_defer_kernel<T, op_t, kThreads, kItems, exclusive, kMinBlocks>;
+  const int per_sm = resident_ctas(k, L::bytes);
+  if(per_sm < 1) return MGPU_ERR_CUDA;
+  const int64_t num_tiles = div_up(count, kTile);
+  const int64_t grid = std::min<int64_t>((int64_t)per_sm * sm_count, num_tiles);
+  k<<<(unsigned)grid, kThreads, L::bytes, stream>>>(in, out, count, init, op_t(), status,
+    counter, reduction, error, vec);
+  return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+}
+
 template<typename T, typename op_t>
 mgpu_status_t launch(cudaStream_t stream, mgpu_scan_type_t scan_type, const void* in, void* out,
-  int64_t count, const void* init_p, void* reduction, uint64_t* scratch) {
+  int64_t count, const void* init_p, void* reduction, uint64_t* scratch, int sm_count) {
   T init = op_t::identity();
   if(init_p) memcpy(&init, init_p, sizeof(T));
   if(count == 0) {
@@ -85,21 +120,19 @@ mgpu_status_t launch(cudaStream_t stream, mgpu_scan_type_t scan_type, const void
   int* error = (int*)(scratch + 1);
   int vec = 0 == (((uintptr_t)in | (uintptr_t)out) & 15);
   if(scan_type == MGPU_SCAN_EXC)
-    scan_kernel<T, op_t, kThreads, kItems, true><<<(unsigned)num_tiles, kThreads, 0, stream>>>(
-      (const T*)in, (T*)out, count, init, op_t(), status, counter, (T*)reduction, error, vec);
-  else
-    scan_kernel<T, op_t, kThreads, kItems, false><<<(unsigned)num_tiles, kThreads, 0, stream>>>(
-      (const T*)in, (T*)out, count, init, op_t(), status, counter, (T*)reduction, error, vec);
-  return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+    return launch_defer<T, op_t, true>(stream, (const T*)in, (T*)out, count, init, (T*)reduction,
+      status, counter, error, vec, sm_count);
+  return launch_defer<T, op_t, false>(stream, (const T*)in, (T*)out, count, init, (T*)reduction,
+    status, counter, error, vec, sm_count);
 }
 
 template<typename T>
 mgpu_status_t by_op(mgpu_op_t op, cudaStream_t s, mgpu_scan_type_t st, const void* in,
-  void* out, int64_t count, const void* init, void* red, uint64_t* scratch) {
+  void* out, int64_t count, const void* init, void* red, uint64_t* scratch, int sm) {
   switch(op) {
-    case MGPU_PLUS: return launch<T, plus_t<T>>(s, st, in, out, count, init, red, scratch);
-    case MGPU_MAX: return launch<T, max_t<T>>(s, st, in, out, count, init, red, scratch);
-    case MGPU_MIN: return launch<T, min_t<T>>(s, st, in, out, count, init, red, scratch);
+    case MGPU_PLUS: return launch<T, plus_t<T>>(s, st, in, out, count, init, red, scratch, sm);
+    case MGPU_MAX: return launch<T, max_t<T>>(s, st, in, out, count, init, red, scratch, sm);
+    case MGPU_MIN: return launch<T, min_t<T>>(s, st, in, out, count, init, red, scratch, sm);
   }
   return MGPU_ERR_INVALID_ARG;
 }
@@ -165,10 +198,11 @@ extern "C" mgpu_status_t mgpu_scan_noalloc(void* stream, mgpu_dtype_t type,
   uint64_t* scratch = nullptr;
   if(scratch_address(device, &scratch) != cudaSuccess) return MGPU_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;
+  const int sm = g_sm_count[device];
   switch(type) {
-    case MGPU_I32: return by_op<int32_t>(op, s, scan_type, in, out, count, init, reduction, scratch);
-    case MGPU_U32: return by_op<uint32_t>(op, s, scan_type, in, out, count, init, reduction, scratch);
-    case MGPU_F32: return by_op<float>(op, s, scan_type, in, out, count, init, reduction, scratch);
+    case MGPU_I32: return by_op<int32_t>(op, s, scan_type, in, out, count, init, reduction, scratch, sm);
+    case MGPU_U32: return by_op<uint32_t>(op, s, scan_type, in, out, count, init, reduction, scratch, sm);
+    case MGPU_F32: return by_op<float>(op, s, scan_type, in, out, count, init, reduction, scratch, sm);
     default: break;
   }
   return MGPU_ERR_UNSUPPORTED;
