@@ -17,11 +17,12 @@
 //    The kernel is bound by shared-memory traffic and by how many warps and
 //    keys each SM holds, so it keeps almost nothing per key in registers:
 //    keys are read from the staged tile each time they are needed and ranks
-//    are packed 16-bit pairs.  Each warp ranks its rows of 32 keys (stable,
-//    element order) through one 64-bit mask+count word per digit; the CTA
-//    publishes its per-digit counts and walks back over predecessor tiles'
-//    published counts (decoupled look-back, several predecessors per L2 round
-//    trip, overlapping the scatter) to find its global offset per digit.
+//    are packed 16-bit pairs.  Each half-warp ranks its rows of 16 keys
+//    (stable, element order) through one 32-bit word per digit, a 16-bit
+//    peer mask under a 16-bit running count; the CTA publishes its per-digit
+//    counts and walks back over predecessor tiles' published counts
+//    (decoupled look-back, several predecessors per L2 round trip,
+//    overlapping the scatter) to find its global offset per digit.
 //    Keys are scattered into a second shared-memory region in local digit
 //    order and written out in runs, so global stores coalesce; the values'
 //    bulk copy reuses the first region once the keys have left it, and the
@@ -352,7 +353,7 @@ __device__ __forceinline__ void onesweep_tile(const onesweep_args<K, V>& a,
     reinterpret_cast<uint4*>(mw)[j] = make_uint4(0, 0, 0, 0);
 
   // Concentration of this pass's digits: when some digit holds more than
-  // 1/128 of the keys, rows of 32 equal digits become likely (equal keys sit
+  // 1/128 of the keys, rows of 16 equal digits become likely (equal keys sit
   // together after earlier passes) and the ranking checks for them.  Warp
   // maxima and sums of the digit totals go to scan scratch words 16..31.
   uint32_t hval = 0;
