@@ -21,12 +21,12 @@ mgpu_status_t mergesort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys, 
         return mergesort_kv<NT1, 8, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           greater_t<K>());
       }
-      constexpr int VT_EVEN = sizeof(K) == 4 ? 16 : 8;
+      constexpr int VT2 = sizeof(K) == 4 ? 15 : 8;
       if(variant == 2) {
         if(comp == MGPU_LESS)
-          return mergesort_kv<256, VT_EVEN, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+          return mergesort_kv<256, VT2, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
             less_t<K>());
-        return mergesort_kv<256, VT_EVEN, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
+        return mergesort_kv<256, VT2, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           greater_t<K>());
       }
       if(comp == MGPU_LESS)

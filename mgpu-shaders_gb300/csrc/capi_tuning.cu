@@ -27,7 +27,8 @@ const char* variant_name(int prim, int bytes, int v) {
   switch(prim) {
     case prim_radix: return variants::radix_name(bytes, v);
     case prim_scan: return variants::scan_name(bytes, v);
-    case prim_merge: case prim_mergesort: return variants::merge_name(bytes, v);
+    case prim_merge: return variants::merge_name(bytes, v);
+    case prim_mergesort: return variants::mergesort_name(bytes, v);
   }
   return "";
 }

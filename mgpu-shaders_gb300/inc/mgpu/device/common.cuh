@@ -207,5 +207,21 @@ __device__ __forceinline__ bool aligned16(const void* p) {
   return 0 == ((uintptr_t)p & 15);
 }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialisation attribute may start while the kernel before it on the
+// stream is still running: griddep_wait() returns once that kernel has
+// completed and its memory operations are visible (at once when the launch
+// had no such predecessor), so it must precede every access to memory the
+// predecessor touches.  griddep_launch_dependents() lets the next kernel's
+// CTAs be placed as soon as every CTA of this grid has called it (or exited);
+// calling it after griddep_wait() keeps at most one waiting grid resident.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace device
 }  // namespace mgpu

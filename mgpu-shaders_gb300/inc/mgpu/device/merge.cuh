@@ -352,6 +352,9 @@ mergesort_pass_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_o
   int64_t count, int64_t run, const int64_t* mp, int bulk_ok, comp_t comp, int* error) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NV = NT * VT;
+  // Launched as a dependent of the previous pass (or the blocksort).
+  griddep_wait();
+  griddep_launch_dependents();
   const int64_t tile = blockIdx.x;
   const int64_t pos0 = tile * NV;
   const int64_t pair = pos0 / (2 * run);
@@ -400,6 +403,9 @@ blocksort_kernel(const K* keys_in, const V* vals_in, K* keys_out, V* vals_out, i
   const int tid = threadIdx.x;
   const int64_t base = (int64_t)blockIdx.x * NV;
   const int valid = (int)min((int64_t)NV, count - base);
+  // Launched as a dependent of whatever kernel precedes it on the stream.
+  griddep_wait();
+  griddep_launch_dependents();
 
   // Load the tile (coalesced), then take VT consecutive items per thread.
   constexpr int KV16 = (int)(sizeof(K) * NV / 16);

@@ -182,6 +182,21 @@ __device__ __forceinline__ void group_merge_sort(U* sk, V* sv, int n, int gtid) 
   gsync();
 }
 
+// group_merge_sort with the fewest items per thread, among 3, 7, 13 and
+// ITEMS, whose W warps cover n.  The register sort and every merge step cost
+// in proportion to the items per thread, while a segment's lanes all run
+// the same steps: a 200-key segment sorted by one warp at 21 items per thread
+// keeps 10 lanes busy for 4 merge passes of 21 steps each; at 7 items per
+// thread 29 lanes take 5 passes of 7 steps.
+template<int W, int ITEMS, typename U, typename V>
+__device__ __forceinline__ void group_merge_sort_fit(U* sk, V* sv, int n, int gtid) {
+  constexpr int G = 32 * W;
+  if(ITEMS > 3 && n <= G * 3) group_merge_sort<W, 3>(sk, sv, n, gtid);
+  else if(ITEMS > 7 && n <= G * 7) group_merge_sort<W, 7>(sk, sv, n, gtid);
+  else if(ITEMS > 13 && n <= G * 13) group_merge_sort<W, 13>(sk, sv, n, gtid);
+  else group_merge_sort<W, ITEMS>(sk, sv, n, gtid);
+}
+
 // Shared memory of the in-CTA sorts: the tile's keys (radix bits) and values,
 // scan scratch and a work-item slot.
 template<typename K, typename V, int NT, int ITEMS, int SLICE_ITEMS>
@@ -276,7 +291,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int n = (int)(offsets[seg + 1] - b);
     seg_stage_in<NT>(keys + b, HAS_V ? vals + b : vals, n, ks, vs, tid);
     __syncthreads();
-    group_merge_sort<NT / 32, ITEMS>(ks, vs, n, tid);
+    group_merge_sort_fit<NT / 32, ITEMS>(ks, vs, n, tid);
     for(int i = tid; i < n; i += NT) {
       keys[b + i] = radix_key<K>::from_bits(ks[i]);
       if constexpr(HAS_V) vals[b + i] = vs[i];
@@ -298,7 +313,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
     const int n = (int)(offsets[seg + 1] - b);
     seg_stage_in<32>(keys + b, HAS_V ? vals + b : vals, n, wks, wvs, lane);
     __syncwarp();
-    group_merge_sort<1, SLICE_ITEMS>(wks, wvs, n, lane);
+    group_merge_sort_fit<1, SLICE_ITEMS>(wks, wvs, n, lane);
     for(int i = lane; i < n; i += 32) {
       keys[b + i] = radix_key<K>::from_bits(wks[i]);
       if constexpr(HAS_V) vals[b + i] = wvs[i];

@@ -18,6 +18,7 @@
 #include <map>
 #include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mgpu_gb300.h"
@@ -156,6 +157,28 @@ struct context_t {
     cudaError_t e = cudaGetLastError();
     if(timed) { r.end = acquire_event(); cudaEventRecord(r.end, stream); pending.push_back(r); }
     return check(e) ? MGPU_ERR_CUDA : MGPU_OK;
+  }
+
+  // Enqueues `kernel` on `stream` with programmatic dependent launch allowed
+  // (outside a capture by this context): its CTAs may be placed while the
+  // previous kernel on the stream is still running, so the kernel must call
+  // device::griddep_wait() before it touches memory that kernel uses.  For
+  // chains of short, latency-bound launches (mergesort passes over a few MB)
+  // this hides each launch's ramp behind its predecessor's tail.
+  template<typename... P, typename... A>
+  void enqueue_dependent(void (*kernel)(P...), unsigned grid, unsigned block, size_t smem,
+    A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = capturing ? 0 : 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
   }
 
   // Resolves pending event pairs into per-kernel totals.

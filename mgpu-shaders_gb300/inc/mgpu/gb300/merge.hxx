@@ -61,6 +61,18 @@ template<int key_bytes> struct merge_tuning;
 template<> struct merge_tuning<4> { enum { nt = 256, vt = 15 }; };
 template<> struct merge_tuning<8> { enum { nt = 256, vt = 7 }; };
 
+// Mergesort tiles: 4-byte keys take 17 items per thread where the blocksort's
+// static shared arrays (keys and values of one tile) stay within 48 KB: a
+// 4352-item tile sorts a power-of-two count in one pass fewer than the merge
+// shape's 3840 (2^20 keys: 241 tiles, 8 passes, against 274 tiles and 9).
+template<typename K, typename V> struct mergesort_tuning {
+  static constexpr bool has_values = !std::is_same<V, device::no_values>::value;
+  static constexpr int nt = merge_tuning<sizeof(K)>::nt;
+  static constexpr int vt = sizeof(K) == 4 &&
+    (sizeof(K) + (has_values ? sizeof(V) : 0)) * nt * 17 + sizeof(K) <= 48 * 1024 ? 17 :
+    (int)merge_tuning<sizeof(K)>::vt;
+};
+
 template<int nt = 0, int vt = 0, typename K, typename V, typename comp_t>
 status_t merge_kv(void* aux_data, size_t* aux_size, context_t& ctx,
   const K* a_keys, const V* a_vals, int64_t a_count,
@@ -135,8 +147,8 @@ template<int nt = 0, int vt = 0, bool sort_indices = false, typename K, typename
 status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys, V* vals,
   int64_t count, comp_t comp) {
   using namespace device;
-  constexpr int NT = nt ? nt : (int)merge_tuning<sizeof(K)>::nt;
-  constexpr int VT = vt ? vt : (int)merge_tuning<sizeof(K)>::vt;
+  constexpr int NT = nt ? nt : mergesort_tuning<K, V>::nt;
+  constexpr int VT = vt ? vt : mergesort_tuning<K, V>::vt;
   constexpr int NV = NT * VT;
   constexpr bool has_values = !std::is_same<V, no_values>::value;
   static_assert(!sort_indices || has_values, "indices need a value array");
@@ -163,9 +175,11 @@ status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys,
   V* vb = (num_passes & 1) ? v2 : vals;
   const int vec = aligned16_host(keys) && aligned16_host(kb) &&
     (!has_values || (aligned16_host(vals) && aligned16_host(vb)));
+  // The blocksort and the passes are launched as programmatic dependents
+  // (each kernel waits for its predecessor in its first instruction).
   st = ctx.launch("blocksort", [&] {
-    blocksort_kernel<K, V, NT, VT, sort_indices, comp_t><<<(unsigned)num_tiles, NT, 0,
-      ctx.stream>>>(keys, vals, kb, vb, count, comp, vec);
+    ctx.enqueue_dependent(blocksort_kernel<K, V, NT, VT, sort_indices, comp_t>,
+      (unsigned)num_tiles, NT, 0, (const K*)keys, (const V*)vals, kb, vb, count, comp, vec);
   });
   if(st || !num_passes) return st;
 
@@ -188,8 +202,9 @@ status_t mergesort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* keys,
     }
     int bulk = aligned16_host(kin) && (!has_values || aligned16_host(vin));
     st = ctx.launch("mergesort_pass", [&] {
-      kernel<<<(unsigned)num_tiles, NT, L::bytes, ctx.stream>>>(kin, vin, kout, vout, count, run,
-        fused ? nullptr : mp, bulk, comp, ctx.d_error);
+      ctx.enqueue_dependent(kernel, (unsigned)num_tiles, NT, L::bytes, (const K*)kin,
+        (const V*)vin, kout, vout, count, run, (const int64_t*)(fused ? nullptr : mp), bulk,
+        comp, ctx.d_error);
     });
     if(st) return st;
     std::swap(kin, kout);
