@@ -21,7 +21,7 @@ mgpu_status_t mergesort_w32(mgpu_context* c, mgpu_dtype_t key_type, void* keys, 
         return mergesort_kv<NT1, 8, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,
           greater_t<K>());
       }
-      constexpr int VT2 = sizeof(K) == 4 ? 15 : 8;
+      constexpr int VT2 = mergesort_tuning<K, V>::vt_alt;
       if(variant == 2) {
         if(comp == MGPU_LESS)
           return mergesort_kv<256, VT2, I>(aux, aux_size, c->ctx, (K*)keys, (V*)vals, count,

@@ -37,11 +37,11 @@ inline const char* merge_name(int bytes, int v) {
   static const char* n8[] = { "256x7", "128x8", "256x8" };
   return bytes == 4 ? n4[v] : n8[v];
 }
-// mergesort: 4-byte keys {256x17 (256x15 with 8-byte values, whose tile
-// would not fit the blocksort's 48 KB of static shared memory), 256x8,
-// 256x15}; 8-byte keys as merge.
+// mergesort: 4-byte keys {256x15, 256x8, 256x17 (256x15 with 8-byte values,
+// whose tile would not fit the blocksort's 48 KB of static shared memory)};
+// 8-byte keys as merge.
 inline const char* mergesort_name(int bytes, int v) {
-  static const char* n4[] = { "256x17", "256x8", "256x15" };
+  static const char* n4[] = { "256x15", "256x8", "256x17" };
   return bytes == 4 ? n4[v] : merge_name(bytes, v);
 }
 

@@ -61,16 +61,18 @@ template<int key_bytes> struct merge_tuning;
 template<> struct merge_tuning<4> { enum { nt = 256, vt = 15 }; };
 template<> struct merge_tuning<8> { enum { nt = 256, vt = 7 }; };
 
-// Mergesort tiles: 4-byte keys take 17 items per thread where the blocksort's
-// static shared arrays (keys and values of one tile) stay within 48 KB: a
-// 4352-item tile sorts a power-of-two count in one pass fewer than the merge
-// shape's 3840 (2^20 keys: 241 tiles, 8 passes, against 274 tiles and 9).
+// Mergesort shapes: the merge shape by default.  `vt_alt` (a tuning variant)
+// gives 4-byte keys 17 items per thread where the blocksort's static shared
+// arrays (keys and values of one tile) stay within 48 KB: a 4352-item tile
+// sorts a power-of-two count in one pass fewer than 3840 (2^20 keys: 8
+// passes instead of 9), but each pass costs more, so it wins at 2^20 u32 kv
+// (0.1034 against 0.1055 ms) and loses at 2^24 (0.986 against 0.957 ms).
 template<typename K, typename V> struct mergesort_tuning {
   static constexpr bool has_values = !std::is_same<V, device::no_values>::value;
   static constexpr int nt = merge_tuning<sizeof(K)>::nt;
-  static constexpr int vt = sizeof(K) == 4 &&
-    (sizeof(K) + (has_values ? sizeof(V) : 0)) * nt * 17 + sizeof(K) <= 48 * 1024 ? 17 :
-    (int)merge_tuning<sizeof(K)>::vt;
+  static constexpr int vt = merge_tuning<sizeof(K)>::vt;
+  static constexpr int vt_alt = sizeof(K) == 4 &&
+    (sizeof(K) + (has_values ? sizeof(V) : 0)) * nt * 17 + sizeof(K) <= 48 * 1024 ? 17 : vt;
 };
 
 template<int nt = 0, int vt = 0, typename K, typename V, typename comp_t>

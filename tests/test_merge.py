@@ -98,11 +98,11 @@ def run_mergesort(mgpu, ctx, k, v, comp):
     return dk.numpy(), (None if dv is None else dv.numpy())
 
 
-# 4352 = one 256 x 17 tile (u32 keys + u32 values); 2^20 keys take 241 tiles
-# and eight passes.
-@pytest.mark.parametrize("n", [0, 1, 2, 15, 16, 17, 255, 4095, 4096, 4097, 4351, 4352, 4353,
-                               8192, 8193, 8704, 8705, 3 * 4096 + 11, 100_000, 1 << 20,
-                               (1 << 20) + 4352 * 15])
+# 3840 = one 256 x 15 tile (u32 keys + u32 values): 2^20 keys take 274 tiles
+# and nine passes.
+@pytest.mark.parametrize("n", [0, 1, 2, 15, 16, 17, 255, 3839, 3840, 3841, 4095, 4096, 4097,
+                               7680, 7681, 8192, 8193, 3 * 4096 + 11, 100_000, 1 << 20,
+                               (1 << 20) + 3840 * 15])
 def test_mergesort_sizes(mgpu, ctx, oracle, rng, n):
     k = dup_keys(rng, n, np.uint32)
     v = np.arange(n, dtype=np.uint32)
