@@ -407,8 +407,9 @@ def wl_mergesort(args, mg, torch):
     alg = passes * 16 * n
     cfg = {"workload": "mergesort_kv u32 keys + i32 index values, %d keys, std::less" % n,
            "count": n, "alg_bytes_per_key": alg // n,
-           "l2": "8 MiB working set is L2-resident; restored by a device copy outside the "
-                 "step's events"}
+           "l2": "%d MiB of keys and values, %s; restored by a device copy outside the "
+                 "step's events" % (8 * n >> 20, "L2-resident" if 8 * n <= (64 << 20)
+                                    else "larger than L2")}
     return _line("Mkeys/s", "Mkeys/s", n, alg, ms, steps, warmup, launches, clk, roof, kernels,
                  cfg, "u32", checks)
 

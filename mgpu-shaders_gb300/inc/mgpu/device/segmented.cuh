@@ -7,8 +7,8 @@
 //
 //  1. seg_classify: one pass over the offsets puts each segment in a size
 //     class: <= 32 keys (one warp, rank sort in registers), <= 32*items keys
-//     (one warp, LSD radix in a shared-memory slice), <= one tile (one CTA,
-//     LSD radix in shared memory), larger (multi-CTA onesweep).  Large
+//     (one warp, merge sort in a shared-memory slice), <= one tile (one CTA,
+//     merge sort in shared memory), larger (multi-CTA onesweep).  Large
 //     segments get contiguous tile ranges and zeroed histogram rows.
 //  2. seg_small_sort: one persistent launch; CTAs pull CTA-class segments,
 //     then warps pull warp-class segments, from atomic queues.
@@ -257,7 +257,7 @@ radix_sort_cta(K* keys, V* vals, int n) {
   const int tid = threadIdx.x;
   seg_stage_in<NT>(keys, vals, n, ks, vs, tid);
   __syncthreads();
-  group_merge_sort<NT / 32, ITEMS>(ks, vs, n, tid);
+  group_merge_sort_fit<NT / 32, ITEMS>(ks, vs, n, tid);
   for(int i = tid; i < n; i += NT) {
     keys[i] = radix_key<K>::from_bits(ks[i]);
     if constexpr(HAS_V) vals[i] = vs[i];

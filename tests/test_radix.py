@@ -12,10 +12,11 @@ from datagen import wide_keys
 
 pytestmark = pytest.mark.gpu
 
-# Around the one-CTA limits (3072 keys of 8 bytes, 5120 of 4 bytes) and the
-# onesweep tiles (4096 for 8-byte keys or values, 7296 otherwise).
-SIZES = [0, 1, 2, 31, 32, 33, 255, 3072, 3073, 4095, 4096, 4097, 5120, 5121, 7296, 7297,
-         3 * 4096 + 5, 2 * 7296 + 1, 65536 + 7, 300_001]
+# Around the one-CTA limits (3072 keys of 8 bytes, 5120 of 4 bytes; the
+# one-CTA sort takes 3 items per thread up to 3072 keys) and the onesweep
+# tiles (4096 for 8-byte keys or values, 7296 otherwise).
+SIZES = [0, 1, 2, 31, 32, 33, 255, 2560, 2561, 3072, 3073, 4095, 4096, 4097, 5120, 5121, 7296,
+         7297, 3 * 4096 + 5, 2 * 7296 + 1, 65536 + 7, 300_001]
 KEY_TYPES = [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64]
 
 
@@ -47,6 +48,20 @@ def test_radix_sizes(mgpu, ctx, oracle, rng, n, kt):
 @pytest.mark.parametrize("kt", [np.uint32, np.uint64, np.int32])
 def test_radix_distributions(mgpu, ctx, oracle, rng, dist, kt):
     n = 200_003
+    k = gen_keys(rng, n, kt, dist)
+    v = np.arange(n, dtype=np.uint32)
+    gk, gv = run_sort(mgpu, ctx, k, v)
+    ok, ov = oracle.radix_sort(k, v)
+    assert np.array_equal(bits(gk), bits(ok))
+    assert np.array_equal(gv, ov)
+
+
+@pytest.mark.parametrize("dist", ["distinct256", "equal", "two", "sorted", "reverse"])
+@pytest.mark.parametrize("n", [300, 2500, 4000])
+@pytest.mark.parametrize("kt", [np.uint32, np.float32, np.uint64])
+def test_radix_one_cta_distributions(mgpu, ctx, oracle, rng, dist, n, kt):
+    """Sorts that fit one CTA (a merge sort in shared memory) keep equal
+    keys in input order."""
     k = gen_keys(rng, n, kt, dist)
     v = np.arange(n, dtype=np.uint32)
     gk, gv = run_sort(mgpu, ctx, k, v)

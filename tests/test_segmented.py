@@ -36,8 +36,8 @@ def bits(a):
 # Inside a class the items per thread drop to 3, 7 or 13 when those cover the
 # segment: limits 96 / 224 / 416 for a warp, 768 / 1792 / 3328 for a CTA.
 @pytest.mark.parametrize("lens", [
-    [0], [1], [2], [32], [33], [96], [97], [224], [225], [416], [417], [512], [513], [672],
-    [673], [768], [769], [1792], [1793], [3328], [3329],
+    [0], [1], [2], [32], [33], [96], [97], [224], [225], [336], [337], [416], [417], [512],
+    [513], [672], [673], [768], [769], [1792], [1793], [2688], [2689], [3328], [3329],
     [4096], [4097], [5376], [5377], [7297], [2 * 7296 + 5], [0, 5, 0, 70, 1, 0],
     [10_000, 1, 3, 4096, 4097, 100_000, 31, 512, 600],
 ])
