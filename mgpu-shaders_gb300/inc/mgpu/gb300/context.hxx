@@ -160,14 +160,19 @@ struct context_t {
   }
 
   // Enqueues `kernel` on `stream` with programmatic dependent launch allowed
-  // (outside a capture by this context): its CTAs may be placed while the
-  // previous kernel on the stream is still running, so the kernel must call
-  // device::griddep_wait() before it touches memory that kernel uses.  For
-  // chains of short, latency-bound launches (mergesort passes over a few MB)
-  // this hides each launch's ramp behind its predecessor's tail.
+  // (unless the stream is being captured into a graph, by this context or
+  // by its caller): its CTAs may be placed while the previous kernel on the
+  // stream is still running, so the kernel must call device::griddep_wait()
+  // before it touches memory that kernel uses.  For chains of short,
+  // latency-bound launches (mergesort passes over a few MB) this hides each
+  // launch's ramp behind its predecessor's tail.  A failed launch is left
+  // for cudaGetLastError(), which launch() reads.
   template<typename... P, typename... A>
   void enqueue_dependent(void (*kernel)(P...), unsigned grid, unsigned block, size_t smem,
     A&&... args) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const bool captured = capturing ||
+      cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
@@ -177,7 +182,7 @@ struct context_t {
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = capturing ? 0 : 1;
+    cfg.numAttrs = captured ? 0 : 1;
     cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
   }
 
