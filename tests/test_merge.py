@@ -135,6 +135,24 @@ def test_mergesort_distributions(mgpu, ctx, oracle, rng, dist):
     assert np.array_equal(gk, ok) and np.array_equal(gv, ov)
 
 
+@pytest.mark.parametrize("n", [3000, 100_003, 1 << 20])
+def test_mergesorts_chained_without_a_sync(mgpu, ctx, oracle, rng, n):
+    """The blocksort and merge passes start as programmatic dependents of the
+    kernel before them: back-to-back sorts of one array on one stream (a
+    radix sort, then two mergesorts) must each see the previous result."""
+    k = dup_keys(rng, n, np.uint32, hi=700)
+    v = np.arange(n, dtype=np.uint32)
+    dk, dv = dev(mgpu, k), dev(mgpu, v)
+    ctx.radix_sort(dk, dv)
+    ctx.mergesort(dk, dv, comp="greater")
+    ctx.mergesort(dk, dv, comp="less")
+    ctx.synchronize()
+    k1, v1 = oracle.radix_sort(k, v)
+    k2, v2 = oracle.sort(k1, v1, mode="greater")
+    k3, v3 = oracle.sort(k2, v2, mode="less")
+    assert np.array_equal(dk.numpy(), k3) and np.array_equal(dv.numpy(), v3)
+
+
 @pytest.mark.parametrize("n", [1, 10_000, 1 << 20])
 def test_mergesort_indices(mgpu, ctx, oracle, rng, n):
     """vk::mergesort_indices, checked like examples/gl_sort/gl_sort.cxx:18-27:
