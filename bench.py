@@ -1248,8 +1248,9 @@ def main():
 
     e2e_run(2)                   # untimed warm-up of the copy path and the streams
     # Host<->device bandwidth on this machine is shared with other tenants'
-    # jobs: take the median of three timed runs.
-    e2e_runs = [e2e_run(e2e_steps) / e2e_steps for _ in range(3)]
+    # jobs, and a 16-step run of the copies alone varies from 13.3 to 16.4 ms
+    # per step: take the median of five timed runs.
+    e2e_runs = [e2e_run(e2e_steps) / e2e_steps for _ in range(5)]
     e2e_ms = statistics.median(e2e_runs)
     e2e_ok = all(bool(np.array_equal(keys_h[ov.numpy()], ok.numpy())) for ok, ov in outs)
 
