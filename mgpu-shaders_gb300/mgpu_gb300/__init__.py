@@ -33,6 +33,15 @@ def _torch():
     return torch
 
 
+def tuning_variants(primitive, key_dtype):
+    """Names of the compiled launch shapes of `primitive` ("radix", "scan",
+    "merge", "mergesort") for keys of `key_dtype`, in variant order (host
+    only: no device or context needed)."""
+    buf = ctypes.create_string_buffer(512)
+    n = lib().mgpu_tuning_variants(PRIMITIVES[primitive], DTYPES[np.dtype(key_dtype)], buf, 512)
+    return buf.value.decode().split("\n")[:n]
+
+
 class DeviceArray:
     """A device buffer of `count` elements of a numpy dtype, held by a torch
     uint8 tensor.  Only its pointer is handed to the library."""
@@ -140,9 +149,7 @@ class Context:
 
     # --- launch-shape tuning ---
     def tuning_variants(self, primitive, key_dtype):
-        buf = ctypes.create_string_buffer(512)
-        n = lib().mgpu_tuning_variants(PRIMITIVES[primitive], DTYPES[np.dtype(key_dtype)], buf, 512)
-        return buf.value.decode().split("\n")[:n]
+        return tuning_variants(primitive, key_dtype)
 
     def tuning_set(self, primitive, key_dtype, val_bytes, bucket, variant):
         self._check(lib().mgpu_tuning_set(self._h, PRIMITIVES[primitive],
