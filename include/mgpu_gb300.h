@@ -246,6 +246,11 @@ MGPU_API mgpu_status_t mgpu_tuning_set(mgpu_context_t* ctx, int primitive,
 /* Variant the context would use for this call shape. */
 MGPU_API int mgpu_tuning_get(mgpu_context_t* ctx, int primitive, mgpu_dtype_t key_type,
   int val_bytes, int64_t count);
+/* Tables persist as text, one "primitive key_type val_bytes size_bucket
+ * variant" line per entry ('#' starts a comment line).  Loading adds the
+ * file's entries to the context's table only if every entry names a
+ * compiled variant and a bucket in -1..62; otherwise it returns
+ * MGPU_ERR_INVALID_ARG and the table is unchanged. */
 MGPU_API mgpu_status_t mgpu_tuning_save(mgpu_context_t* ctx, const char* path);
 MGPU_API mgpu_status_t mgpu_tuning_load(mgpu_context_t* ctx, const char* path);
 /* Times every variant on device-generated data of this type and size (median

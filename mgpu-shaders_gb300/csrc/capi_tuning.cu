@@ -110,7 +110,19 @@ mgpu_status_t mgpu_tuning_save(mgpu_context_t* c, const char* path) {
 mgpu_status_t mgpu_tuning_load(mgpu_context_t* c, const char* path) {
   MGPU_CHECK_CTX(c);
   if(!path) return MGPU_ERR_INVALID_ARG;
-  return c->ctx.tuning.load(path) ? MGPU_OK : MGPU_ERR_INVALID_ARG;
+  // Read into a scratch table and take it only if every entry names a
+  // compiled variant and a valid bucket, so a bad file changes nothing.
+  tuning_table_t t;
+  if(!t.load(path)) return MGPU_ERR_INVALID_ARG;
+  for(auto& e : t.entries) {
+    const int prim = std::get<0>(e.first), type = std::get<1>(e.first);
+    const int bucket = std::get<3>(e.first);
+    if(type < 0 || type > MGPU_F64 || bucket < -1 || bucket > 62 || e.second < 0 ||
+       e.second >= variant_count(prim, variants::dtype_bytes((mgpu_dtype_t)type)))
+      return MGPU_ERR_INVALID_ARG;
+  }
+  for(auto& e : t.entries) c->ctx.tuning.entries[e.first] = e.second;
+  return MGPU_OK;
 }
 
 mgpu_status_t mgpu_autotune(mgpu_context_t* c, int primitive, mgpu_dtype_t key_type,

@@ -67,3 +67,21 @@ def test_scan_rejects_an_operator_not_declared_commutative(tmp_path):
     assert r.returncode != 0 and "commutative" in r.stdout + r.stderr
     r = subprocess.run(base[:1] + ["-DOPT_IN"] + base[1:], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_tuning_table_host_logic(tmp_path):
+    """The tuning table (size buckets, lookup precedence, text round trip,
+    malformed lines) is host code: compiled with the host compiler and run
+    without a GPU."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no host C++ compiler")
+    exe = str(tmp_path / "tuning_table")
+    subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Werror",
+                    "-I", os.path.join(REPO, "mgpu-shaders_gb300", "inc"),
+                    os.path.join(HERE, "cpp", "tuning_table.cpp"), "-o", exe],
+                   check=True, capture_output=True, text=True)
+    r = subprocess.run([exe, str(tmp_path / "table.txt")], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 0 and "ok tuning_table" in r.stdout, r.stdout + r.stderr
+

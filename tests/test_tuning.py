@@ -79,6 +79,29 @@ def test_autotune_records_and_round_trips(mgpu, tmp_path):
     c2.close()
 
 
+def test_tuning_load_rejects_a_bad_file_whole(mgpu, tmp_path):
+    """A table naming a variant that is not compiled (or a bad bucket) is
+    refused and leaves the context's table as it was."""
+    c = mgpu.Context(0)
+    try:
+        c.tuning_set("radix", np.uint32, 4, 20, 2)
+        good = tmp_path / "good.txt"
+        good.write_text("# comment\n0 1 4 22 1\n")
+        c.tuning_load(str(good))
+        assert c.tuning_get("radix", np.uint32, 4, 1 << 22) == 1
+        for body in ("0 1 4 23 1\n0 1 4 24 9\n", "0 1 4 70 1\n", "3 1 4 -1 -1\n"):
+            bad = tmp_path / "bad.txt"
+            bad.write_text(body)
+            with pytest.raises(mgpu.MgpuError):
+                c.tuning_load(str(bad))
+            assert c.tuning_get("radix", np.uint32, 4, 1 << 23) == 0   # nothing taken
+        assert c.tuning_get("radix", np.uint32, 4, 1 << 20) == 2
+        with pytest.raises(mgpu.MgpuError):
+            c.tuning_load(str(tmp_path / "missing.txt"))
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("kt", [np.uint32, np.int32, np.float32, np.uint64, np.float64])
 @pytest.mark.parametrize("vb", [0, 4, 8])
 def test_4bit_digit_variants_are_exact(mgpu, ctx, oracle, rng, kt, vb):
