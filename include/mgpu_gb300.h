@@ -230,7 +230,8 @@ MGPU_API mgpu_status_t mgpu_segmented_scan(mgpu_context_t* ctx, mgpu_dtype_t typ
  * compiled; a per-context table picks one per (primitive, key type, value
  * width, size bucket = ceil(log2 count)), bucket -1 meaning every size.
  * The environment variable MGPU_TUNE_FILE names a table loaded at context
- * creation. */
+ * creation (there, an entry that names no compiled variant runs the default
+ * shape). */
 typedef enum mgpu_primitive_t {
   MGPU_PRIM_RADIX = 0,
   MGPU_PRIM_SCAN = 1,
