@@ -214,7 +214,11 @@ MGPU_API mgpu_status_t mgpu_transform_saxpy_f32(mgpu_context_t* ctx, float a, co
  * over CSR segments, one launch sequence for all segments) ----
  * `offsets` is a device array of num_segments + 1 int64 begin offsets;
  * segment s is [offsets[s], offsets[s+1]).  Keys are sorted in radix order
- * (as mgpu_radix_sort) within each segment; vals follow. */
+ * (as mgpu_radix_sort) within each segment; vals follow.  The offsets must
+ * not decrease and must lie in [0, count]; mgpu_segmented_sort checks that
+ * on the device and otherwise sorts nothing and records
+ * MGPU_ERR_INVALID_ARG for mgpu_synchronize (the segmented scan only marks
+ * heads inside [0, count)). */
 MGPU_API mgpu_status_t mgpu_segmented_sort(mgpu_context_t* ctx, mgpu_dtype_t key_type, void* keys,
   int val_bytes, void* vals, int64_t count, const int64_t* offsets,
   int64_t num_segments, void* aux_data, size_t* aux_size);

@@ -14,6 +14,7 @@ namespace device {
 // to mgpu_status_t on the host.
 enum : int {
   err_none = 0,
+  err_invalid_arg = 1,
   err_lookback_timeout = 3,
 };
 

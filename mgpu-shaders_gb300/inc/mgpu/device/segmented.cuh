@@ -41,18 +41,31 @@ struct seg_state_t {
   int64_t max_tiles;         // bound on the large segments' tiles
 };
 
+// sc_bad: set when the offsets are not a non-decreasing sequence inside
+// [0, count]; every later kernel of the sort then returns at once.
 enum seg_counter_t {
   sc_warp = 0, sc_slice, sc_cta, sc_large, sc_tiles,
-  sc_next_cta, sc_next_warp, sc_next_slice, sc_pass_tiles /* + pass */, sc_count = sc_pass_tiles + 8
+  sc_next_cta, sc_next_warp, sc_next_slice, sc_bad, sc_pass_tiles /* + pass */,
+  sc_count = sc_pass_tiles + 8
 };
 
 // CTA_MAX: the largest segment one CTA sorts in shared memory; larger
-// segments are cut into onesweep tiles of LARGE_TILE keys.
+// segments are cut into onesweep tiles of LARGE_TILE keys.  Offsets outside
+// [0, count] or decreasing would make segments overlap or leave the keys:
+// the sort is then not done (sc_bad) and the context's error word reports
+// MGPU_ERR_INVALID_ARG.  With offsets[s] <= offsets[s + 1] for every s and
+// both ends inside [0, count], the segments tile [offsets[0], offsets[n]).
 template<int CTA_MAX, int LARGE_TILE, int SLICE, int PASSES>
-__global__ void seg_classify(const int64_t* offsets, int64_t num_segments, seg_state_t s) {
+__global__ void seg_classify(const int64_t* offsets, int64_t num_segments, int64_t count,
+  seg_state_t s, int* error) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_segments; i += stride) {
     int64_t b = offsets[i], e = offsets[i + 1];
+    if(b < 0 || e < b || e > count) {
+      atomicOr(&s.counters[sc_bad], 1u);
+      raise_error(error, err_invalid_arg);
+      continue;
+    }
     int64_t n = e - b;
     if(n <= 1) continue;
     if(n <= 32) {
@@ -277,9 +290,11 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
   V* vs = (V*)(smem + L::vals_off);
   int* s_item = (int*)(smem + L::misc_off);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // Bad offsets (sc_bad): no segment is sorted.
+  const bool bad = s.counters[sc_bad] != 0;
 
   // CTA-class segments.
-  const uint32_t num_cta = s.counters[sc_cta];
+  const uint32_t num_cta = bad ? 0 : s.counters[sc_cta];
   while(true) {
     if(tid == 0) *s_item = (int)atomicAdd(&s.counters[sc_next_cta], 1u);
     __syncthreads();
@@ -300,7 +315,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
   }
 
   // Slice-class segments: each warp sorts its own in a private slice.
-  const uint32_t num_slice = s.counters[sc_slice];
+  const uint32_t num_slice = bad ? 0 : s.counters[sc_slice];
   U* wks = ks + warp * L::slice;
   V* wvs = vs + warp * L::slice;
   while(true) {
@@ -322,7 +337,7 @@ seg_small_sort(K* keys, V* vals, const int64_t* offsets, seg_state_t s) {
   }
 
   // Warp-class segments: rank sort in registers.
-  const uint32_t num_warp = s.counters[sc_warp];
+  const uint32_t num_warp = bad ? 0 : s.counters[sc_warp];
   while(true) {
     int item = 0;
     if(lane == 0) item = (int)atomicAdd(&s.counters[sc_next_warp], 1u);
@@ -354,6 +369,7 @@ seg_histogram(const K* keys, const int64_t* offsets, seg_state_t s) {
   __shared__ uint32_t sh[BINS * COPIES];
   const int tid = threadIdx.x;
   const int copy = 0;
+  if(s.counters[sc_bad]) return;
   const int num_tiles = (int)s.counters[sc_tiles];
   const int per = (int)div_up(num_tiles, gridDim.x);
   const int t0 = blockIdx.x * per, t1 = min(num_tiles, t0 + per);
@@ -419,7 +435,7 @@ __global__ void __launch_bounds__(NT, MIN_BLOCKS)
 seg_onesweep_pass(onesweep_args<K, V> a, const int64_t* offsets, seg_state_t s, int pass) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int TILE = NT * ITEMS;
-  if(blockIdx.x >= s.counters[sc_tiles]) return;
+  if(s.counters[sc_bad] || blockIdx.x >= s.counters[sc_tiles]) return;
   const int tile = onesweep_begin<K, V, NT, ITEMS>(a.tile_counter, smem);
   const int l = s.tile_owner[tile];
   const int seg = s.large_seg[l];

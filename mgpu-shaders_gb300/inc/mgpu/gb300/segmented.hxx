@@ -93,7 +93,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   int cgrid = (int)std::min<int64_t>(div_up(num_segments, 256), (int64_t)ctx.sm_count * 8);
   st = ctx.launch("seg_classify", [&] {
     seg_classify<TILE, OTILE, SLICE, PASSES><<<cgrid, 256, 0, ctx.stream>>>(offsets,
-      num_segments, s);
+      num_segments, count, s, ctx.d_error);
   });
   if(st) return st;
 
