@@ -8,8 +8,11 @@
 // vk/mergesort.hxx:10-103.  One tile fits in one CTA: blocksort in place, no
 // aux.  Otherwise: aux = partitions + key/value ping-pong buffers; blocksort
 // into the buffer chosen by the parity of the pass count so that the last
-// pass lands in the caller's arrays (vk/mergesort.hxx:47-59); then per pass a
-// partition launch and a merge launch over pairs of sorted runs.
+// pass lands in the caller's arrays (vk/mergesort.hxx:47-59); then one merge
+// launch per pass over pairs of sorted runs, which finds its own splits up to
+// 8192 tiles and above that follows a partition launch.  The blocksort and
+// the passes are launched as programmatic dependents of the kernel before
+// them.
 #pragma once
 
 #include "context.hxx"
