@@ -1,6 +1,7 @@
 // mgpu::gb300::segmented_sort / segmented_scan - batched primitives over a
-// CSR segment layout (offsets[s] .. offsets[s+1], int64 device array with
-// offsets[0] == 0 and offsets[num_segments] == count).
+// CSR segment layout (offsets[s] .. offsets[s+1], an int64 device array that
+// does not decrease and lies in [0, count]; the sort checks that on the
+// device and, if it fails, sorts nothing and records MGPU_ERR_INVALID_ARG).
 //
 // No reference counterpart (the reference handles one array per call).  The
 // launch sequence is fixed and independent of the number of segments:
@@ -21,13 +22,16 @@ namespace mgpu {
 namespace gb300 {
 
 // Segments of at most one small-sort tile (nt x vt keys) are merge-sorted in
-// shared memory by one CTA (one warp for those of at most 32 x vt keys).  vt is
+// shared memory by one CTA (one warp for those of at most 32 x vt keys), with
+// vt items per thread for the largest and 3, 7 or 13 for segments those
+// cover (device/segmented.cuh, group_merge_sort_fit).  vt is
 // odd so that threads' runs of vt items start in distinct banks (an even vt
 // shares banks: 16 keys per thread made the kernel 1.6x slower than 21); four
 // CTAs per SM at 64 registers.  By the width of the staged elements (the
-// wider of key and value), as the onesweep shapes.  Measured on 10^5 lognormal segments (u32 keys
-// + values): vt 21 -> 4.47 ms per batch, 19 -> 4.49, 17 -> 4.54, 15 -> 4.62;
-// three CTAs per SM at vt 21 -> 4.60.
+// wider of key and value), as the onesweep shapes.  Measured on 10^5
+// lognormal segments (u32 keys + values), before the fitted items per
+// thread: vt 21 -> 4.47 ms per batch, 19 -> 4.49, 17 -> 4.54, 15 -> 4.62;
+// three CTAs per SM at vt 21 -> 4.60 (with the fitting, 3.83 ms).
 template<int elem_bytes> struct seg_small_tuning;
 template<> struct seg_small_tuning<4> { enum { nt = 256, vt = 21, min_blocks = 4 }; };
 template<> struct seg_small_tuning<8> { enum { nt = 256, vt = 13, min_blocks = 4 }; };
