@@ -39,6 +39,7 @@ struct seg_state_t {
   uint32_t* seg_hist;        // [large][passes][256] digit totals
   uint32_t* lookback;        // [passes][max_tiles][256] look-back words
   int64_t max_tiles;         // bound on the large segments' tiles
+  int64_t max_large;         // bound on the number of large segments
 };
 
 // sc_bad: set when the offsets are not a non-decreasing sequence inside
@@ -75,9 +76,18 @@ __global__ void seg_classify(const int64_t* offsets, int64_t num_segments, int64
     } else if(n <= CTA_MAX) {
       s.cta_list[atomicAdd(&s.counters[sc_cta], 1u)] = (int)i;
     } else {
-      int tiles = (int)div_up(n, LARGE_TILE);
-      int l = (int)atomicAdd(&s.counters[sc_large], 1u);
-      int tb = (int)atomicAdd(&s.counters[sc_tiles], (uint32_t)tiles);
+      const int tiles = (int)div_up(n, LARGE_TILE);
+      const uint32_t lu = atomicAdd(&s.counters[sc_large], 1u);
+      const uint32_t tbu = atomicAdd(&s.counters[sc_tiles], (uint32_t)tiles);
+      // Non-overlapping segments inside [0, count] stay within the bounds the
+      // host sized the lists for; only offsets that fail the check above (in
+      // another segment) can get here past them.
+      if((int64_t)lu >= s.max_large || (int64_t)tbu + tiles > s.max_tiles) {
+        atomicOr(&s.counters[sc_bad], 1u);
+        raise_error(error, err_invalid_arg);
+        continue;
+      }
+      const int l = (int)lu, tb = (int)tbu;
       s.large_seg[l] = (int)i;
       s.large_tile_base[l] = tb;
       for(int t = 0; t < tiles; ++t) s.tile_owner[tb + t] = l;

@@ -91,6 +91,7 @@ status_t segmented_sort_kv(void* aux_data, size_t* aux_size, context_t& ctx, K* 
   s.seg_hist = (uint32_t*)(base + hist_off);
   s.lookback = (uint32_t*)(base + lb_off);
   s.max_tiles = max_tiles;
+  s.max_large = max_large;
 
   if(ctx.check(cudaMemsetAsync(s.counters, 0, sizeof(uint32_t) * sc_count, ctx.stream)))
     return MGPU_ERR_CUDA;
